@@ -1,0 +1,175 @@
+/*
+ * mlp_gpu.h -- C-ABI of the GB300 MLP local-search engine (libmlpgpu.so).
+ *
+ * Plain C types only: pointers, sizes and status codes; no CUDA or C++ types
+ * in any signature (a CUDA stream is passed as `void*`).  Every function
+ * returns MLP_OK (0) or a nonzero MLP_ERR_* code; mlp_last_error() gives the
+ * message of the calling thread's last failure.  Handles are not thread-safe:
+ * use one handle per thread, or serialise calls on a handle.
+ *
+ * Mapping to the reference (LabIC-UFF/wamca-gpu-mi):
+ *   mlp_problem_*   MLProblem(costTour, distRound, coordShift) + load()
+ *                   (source/mlproblem.h:61-151, source/mlproblem.cpp:78-207)
+ *   mlp_solver_*    MLSolution (tour, update/costCalc/ldsUpdate, ADS buffer;
+ *                   source/mlsolution.h:62-434) together with the
+ *                   MLKernelSwap / MLKernel2Opt / MLKernelOrOpt tasks
+ *                   (source/mlkernel.h:104-318) and the runKernel/runGpuGpu
+ *                   glue of WAMCAExperiment (source/WamcaExperiment.hpp:229-365)
+ *   mlp_batch_*     many independent DVND searches in shared launches (no
+ *                   counterpart in the reference; the batched form)
+ *   mlp_server_*    continuous-batching request loop (no counterpart; the
+ *                   serving form)
+ * The reference's own extern "C" DVND entry points are in wamca_dvnd.h.
+ *
+ * Conventions: n = number of nodes (node ids 0..n-1, depot 0); size = n + 1 is
+ * the tour length (costTour: the tour starts and ends at depot 0, as in every
+ * reference entry point).  Neighbourhoods: 0 SWAP, 1 2OPT, 2 OROPT1,
+ * 3 OROPT2, 4 OROPT3 (move id = neighbourhood, source/mlads.h:150-181).
+ * `wide` = 0 computes costs and deltas in 32 bits with the reference's
+ * wrap-around arithmetic; `wide` = 1 computes them exactly in 64 bits.
+ */
+#ifndef MLP_GPU_H
+#define MLP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MLP_API __attribute__((visibility("default")))
+#else
+#define MLP_API
+#endif
+
+enum {
+  MLP_OK = 0,
+  MLP_ERR_ARG = 1,         /* invalid argument */
+  MLP_ERR_CUDA = 2,        /* CUDA runtime error (message in mlp_last_error) */
+  MLP_ERR_RANGE = 3,       /* size, distance or coordinate out of range */
+  MLP_ERR_IO = 4,          /* file cannot be read */
+  MLP_ERR_FORMAT = 5,      /* malformed or unsupported instance file */
+  MLP_ERR_NOMEM = 6,       /* device or host allocation failed / over budget */
+  MLP_ERR_STATE = 7,       /* call not valid in the handle's current state */
+  MLP_ERR_UNSUPPORTED = 8  /* feature the reference does not support */
+};
+
+enum { MLP_NB_SWAP = 0, MLP_NB_2OPT = 1, MLP_NB_OROPT1 = 2, MLP_NB_OROPT2 = 3, MLP_NB_OROPT3 = 4 };
+#define MLP_NB_ALL 0x1f
+
+typedef struct mlp_problem* mlp_problem_t;
+typedef struct mlp_solver* mlp_solver_t;
+typedef struct mlp_batch* mlp_batch_t;
+typedef struct mlp_server* mlp_server_t;
+
+typedef struct {
+  int64_t cost;        /* latency of the final tour */
+  int64_t iterations;  /* DVND iterations that applied at least one move */
+  int64_t sweeps;      /* full neighbourhood evaluations run */
+  int64_t moves;       /* moves applied */
+  int64_t evals;       /* move evaluations performed */
+  int32_t converged;   /* 1 if a local optimum was reached */
+  int32_t reserved;
+} mlp_dvnd_stats_t;
+
+/* ---- library ---- */
+MLP_API int mlp_version(void);
+MLP_API const char* mlp_last_error(void);
+MLP_API const char* mlp_status_string(int status);
+MLP_API int mlp_device_count(int32_t* count);
+MLP_API int mlp_set_device(int32_t device);
+
+/* ---- problem (MLProblem) ---- */
+/* Distances D[a][b] = int(sqrtf(float(dx^2+dy^2)) + 0.5*dist_round), built on
+ * the device (source/mlproblem.cpp:153-166).  cost_tour must be 1. */
+MLP_API int mlp_problem_create_coords(int32_t n, const int32_t* x, const int32_t* y,
+                                      int32_t cost_tour, int32_t dist_round, mlp_problem_t* out);
+/* Same with x, y already in device memory. */
+MLP_API int mlp_problem_create_coords_device(int32_t n, const int32_t* x_dev, const int32_t* y_dev,
+                                             int32_t cost_tour, int32_t dist_round,
+                                             mlp_problem_t* out);
+/* Symmetric n x n row-major matrix, entries in [0, 65535]. */
+MLP_API int mlp_problem_create_matrix(int32_t n, const int32_t* dist, int32_t cost_tour,
+                                      mlp_problem_t* out);
+/* TSPLIB EUC_2D file (MLProblem::load). */
+MLP_API int mlp_problem_load_tsplib(const char* path, int32_t cost_tour, int32_t dist_round,
+                                    mlp_problem_t* out);
+MLP_API int mlp_problem_info(mlp_problem_t p, int32_t* n, int32_t* size, int32_t* max_dist);
+/* Copies the n x n distance matrix to host memory. */
+MLP_API int mlp_problem_get_dist(mlp_problem_t p, int32_t* dist);
+MLP_API void mlp_problem_destroy(mlp_problem_t p);
+
+/* ---- solver (MLSolution + MLKernel tasks of one instance) ---- */
+MLP_API int mlp_solver_create(mlp_problem_t p, int32_t wide, mlp_solver_t* out);
+MLP_API void mlp_solver_destroy(mlp_solver_t s);
+/* Stream on which every later call of this solver runs (NULL: the solver's own). */
+MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
+/* Sweep tile shape index (0..5) and DVND iterations per CUDA-graph replay. */
+MLP_API int mlp_solver_set_tile_shape(mlp_solver_t s, int32_t shape);
+MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t iterations);
+/* Tour of `len` = size entries: tour[0] = tour[size-1] = 0 and a permutation of
+ * 1..n-1 in between.  Rebuilds the ADS (update() + ldsUpdate()). */
+MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len);
+/* Same with the tour already in device memory (enqueued, no host sync). */
+MLP_API int mlp_solver_set_tour_device(mlp_solver_t s, const int32_t* tour_dev, int32_t len);
+MLP_API int mlp_solver_get_tour(mlp_solver_t s, int32_t* tour, int32_t len);
+/* Device pointer to the solver's current tour (valid until destroy). */
+MLP_API int mlp_solver_tour_device(mlp_solver_t s, int32_t** tour_dev);
+/* Latency cost of the current tour (MLSolution::costCalc after update). */
+MLP_API int mlp_solver_cost(mlp_solver_t s, int64_t* cost);
+/* Adjacent weights w[p] (MLSolution::weights), `len` = size. */
+MLP_API int mlp_solver_weights(mlp_solver_t s, int32_t* w, int32_t len);
+/* Reference ADS buffer (MLSolution::adsData after ldsUpdate, source/mlads.h:38-74):
+ * 32 + size*(size+3) uint32 words.  Header words 6..31 are zero. */
+MLP_API int mlp_solver_ads(mlp_solver_t s, uint32_t* ads, int64_t words);
+/* Per-block candidates of one neighbourhood on the current tour (the move buffer
+ * an ODC kernel writes, one per reference block), without merging.  Arrays of
+ * mlp_solver_num_candidates(nb) entries; a block without a selectable move gets
+ * cost = INT32_MAX (wide: INT64_MAX) and i = j = 0. */
+MLP_API int mlp_solver_num_candidates(mlp_solver_t s, int32_t nb, int32_t* count);
+MLP_API int mlp_solver_eval(mlp_solver_t s, int32_t nb, int64_t* cost, int32_t* i, int32_t* j);
+/* One reference neighbourhood pass (runKernel: evaluate nb, GPU merge, apply the
+ * kept improving moves, update).  Writes up to max_moves applied moves in
+ * application order; *count = moves applied; *new_cost = resulting cost. */
+MLP_API int mlp_solver_pass(mlp_solver_t s, int32_t nb, int32_t max_moves, int32_t* ids,
+                            int32_t* is, int32_t* js, int64_t* costs, int32_t* count,
+                            int64_t* new_cost);
+/* Multi-improvement DVND to a local optimum over the neighbourhoods of nb_mask
+ * (at most max_iters sweeps).  Synchronous. */
+MLP_API int mlp_solver_dvnd(mlp_solver_t s, int32_t nb_mask, int32_t max_iters,
+                            mlp_dvnd_stats_t* stats);
+/* Enqueue `iterations` DVND iterations on the solver's stream without waiting
+ * (call mlp_solver_begin first; read results with mlp_solver_stats). */
+MLP_API int mlp_solver_begin(mlp_solver_t s, int32_t nb_mask, int32_t max_iters);
+MLP_API int mlp_solver_enqueue(mlp_solver_t s, int32_t iterations);
+MLP_API int mlp_solver_stats(mlp_solver_t s, mlp_dvnd_stats_t* stats);
+/* Enqueue `repeats` evaluation-only sweeps of nb_mask (timing helper; the tour
+ * is not changed).  *evals_per_sweep = move evaluations of one sweep. */
+MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats,
+                             int64_t* evals_per_sweep);
+/* Autotune the sweep tile shape on the current tour; returns the chosen index. */
+MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape);
+
+/* ---- batched form ---- */
+MLP_API int mlp_batch_create(int32_t wide, mlp_batch_t* out);
+MLP_API void mlp_batch_destroy(mlp_batch_t b);
+MLP_API int mlp_batch_set_stream(mlp_batch_t b, void* cuda_stream);
+/* Adds a search of problem p from `tour` (size entries).  The problem must
+ * outlive the batch.  Returns the job index in *job. */
+MLP_API int mlp_batch_add(mlp_batch_t b, mlp_problem_t p, const int32_t* tour, int32_t len,
+                          int32_t* job);
+/* Runs every job's DVND to a local optimum (at most max_iters sweeps each). */
+MLP_API int mlp_batch_run(mlp_batch_t b, int32_t nb_mask, int32_t max_iters);
+/* Resets every job to the tour it was added with (for repeated runs). */
+MLP_API int mlp_batch_reset(mlp_batch_t b);
+MLP_API int mlp_batch_result(mlp_batch_t b, int32_t job, int32_t* tour, int32_t len,
+                             mlp_dvnd_stats_t* stats);
+MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,285 @@
+"""ctypes wrapper of the oracle (oracle/liboracle.so) -- TEST INFRASTRUCTURE.
+
+The oracle is the CPU restatement of the reference's MLP local-search path
+(see mlp_oracle.h).  Only tests/, __graft_entry__.smoke() and the CPU-baseline
+leg of bench.py use it, always as the checker or the timed CPU baseline; the
+GPU engine never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libmlref.so")
+
+_lib: Optional[C.CDLL] = None
+
+
+def build(force: bool = False) -> str:
+    src = [os.path.join(HERE, f) for f in ("mlp_oracle.cpp", "mlp_oracle.h", "Makefile")]
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
+        subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    return LIB
+
+
+def build_ref() -> Optional[str]:
+    """Compiles the reference's CPU evaluator into _ref/ (only where the
+    reference sources are mounted); returns the library path or None."""
+    ref_src = os.environ.get("REF_SRC", "/root/reference/source")
+    if not os.path.isdir(ref_src):
+        return REF_LIB if os.path.exists(REF_LIB) else None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
+    return REF_LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
+        sig = {
+            "orc_mt_rand": (None, [C.c_uint32, i32, vp]),
+            "orc_mt_rand_max": (None, [C.c_uint32, C.c_uint32, i32, vp]),
+            "orc_tsplib_read": (i32, [C.c_char_p, i32, vp, vp]),
+            "orc_dist_from_coords": (None, [i32, vp, vp, i32, vp]),
+            "orc_random_tour": (None, [i32, vp, i32, C.c_uint32, C.c_float, vp]),
+            "orc_cost": (i64, [i32, vp, i32, vp, i32, vp]),
+            "orc_ads_build": (None, [i32, vp, i32, vp, vp, vp, i32, i32, vp]),
+            "orc_num_blocks": (i32, [i32, i32]),
+            "orc_num_threads": (i32, [i32, i32]),
+            "orc_eval": (None, [i32, i32, vp, i32, vp, i32, i32, vp, vp, vp, vp]),
+            "orc_move_delta_bruteforce": (i64, [i32, i32, i32, i32, vp, i32, vp, i32]),
+            "orc_move_delta": (i64, [i32, i32, i32, i32, vp, i32, vp, i32]),
+            "orc_can_merge_same": (i32, [i32, i32, i32, i32, i32, i32, i32]),
+            "orc_can_merge": (i32, [i32, i32, i32, i32, i32, i32]),
+            "orc_merge_same": (i32, [i32, i32, vp, vp, vp, vp]),
+            "orc_merge_cross": (i32, [i32, vp, vp, vp, vp, vp]),
+            "orc_apply": (None, [i32, i32, i32, i32, vp]),
+            "orc_pass": (i32, [i32, i32, vp, i32, vp, i32, i32, vp, vp, vp, vp, vp]),
+            "orc_dvnd": (i32, [i32, vp, i32, vp, i32, i32, vp, i32, i32, vp, vp, vp]),
+            "orc_sweep": (i64, [i32, vp, i32, vp, i32, i32, vp, i32, vp, vp, vp]),
+            "orc_legacy_no_conflict": (i32, [i32, i32, i32, i32, i32, i32]),
+            "orc_legacy_better_no_conflict": (i32, [i32, vp, vp, vp, vp, vp, vp, i32, i32]),
+            "orc_legacy_apply_moves": (C.c_uint32, [i32, vp, i32, vp, i32, vp, vp, vp]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+
+
+def mt_rand(seed: int, count: int) -> np.ndarray:
+    out = np.zeros(count, np.uint32)
+    lib().orc_mt_rand(seed, count, _p(out))
+    return out
+
+
+def mt_rand_max(seed: int, mx: int, count: int) -> np.ndarray:
+    out = np.zeros(count, np.uint32)
+    lib().orc_mt_rand_max(seed, mx, count, _p(out))
+    return out
+
+
+def read_tsplib(path: str, maxn: int = 20000):
+    x = np.zeros(maxn, np.int32)
+    y = np.zeros(maxn, np.int32)
+    n = lib().orc_tsplib_read(path.encode(), maxn, _p(x), _p(y))
+    if n < 0:
+        raise IOError(f"tsplib read failed ({n}): {path}")
+    return x[:n].copy(), y[:n].copy()
+
+
+def dist(x, y, dist_round: bool) -> np.ndarray:
+    x, y = _i32(x), _i32(y)
+    n = len(x)
+    D = np.zeros((n, n), np.int32)
+    lib().orc_dist_from_coords(n, _p(x), _p(y), int(dist_round), _p(D))
+    return D
+
+
+def random_tour(D: np.ndarray, seed: int, alpha: float = 0.5) -> np.ndarray:
+    D = _i32(D)
+    n = D.shape[0]
+    t = np.zeros(n + 1, np.int32)
+    lib().orc_random_tour(n, _p(D), 1, seed, C.c_float(alpha), _p(t))
+    return t
+
+
+def cost(tour, D, wide: bool = False) -> int:
+    t, D = _i32(tour), _i32(D)
+    return int(lib().orc_cost(len(t), _p(t), D.shape[0], _p(D), int(wide), None))
+
+
+def weights(tour, D) -> np.ndarray:
+    t, D = _i32(tour), _i32(D)
+    w = np.zeros(len(t), np.int32)
+    lib().orc_cost(len(t), _p(t), D.shape[0], _p(D), 0, _p(w))
+    return w
+
+
+def ads(tour, D, x, y, dist_round: bool) -> np.ndarray:
+    t, D, x, y = _i32(tour), _i32(D), _i32(x), _i32(y)
+    size = len(t)
+    out = np.zeros(32 + size * (size + 3), np.uint32)
+    lib().orc_ads_build(size, _p(t), D.shape[0], _p(D), _p(x), _p(y), 1, int(dist_round), _p(out))
+    return out
+
+
+def num_blocks(nb: int, size: int) -> int:
+    return int(lib().orc_num_blocks(nb, size))
+
+
+def num_threads(nb: int, size: int) -> int:
+    return int(lib().orc_num_threads(nb, size))
+
+
+def evals_per_sweep(size: int, nbs: Sequence[int] = range(5)) -> int:
+    return sum(num_blocks(nb, size) * num_threads(nb, size) for nb in nbs)
+
+
+def eval_nb(nb: int, tour, D, wide: bool = False, faithful: bool = False):
+    t, D = _i32(tour), _i32(D)
+    m = num_blocks(nb, len(t))
+    c = np.zeros(m, np.int64)
+    i = np.zeros(m, np.int32)
+    j = np.zeros(m, np.int32)
+    ctx = np.zeros(m, np.int32)
+    lib().orc_eval(nb, len(t), _p(t), D.shape[0], _p(D), int(wide), int(faithful), _p(c), _p(i), _p(j), _p(ctx))
+    return c, i, j, ctx
+
+
+def move_delta(mid: int, i: int, j: int, tour, D, wide: bool = False, brute: bool = False) -> int:
+    t, D = _i32(tour), _i32(D)
+    f = lib().orc_move_delta_bruteforce if brute else lib().orc_move_delta
+    return int(f(mid, i, j, len(t), _p(t), D.shape[0], _p(D), int(wide)))
+
+
+def can_merge(m1, m2) -> bool:
+    return bool(lib().orc_can_merge(m1[0], m1[1], m1[2], m2[0], m2[1], m2[2]))
+
+
+def can_merge_same(nb: int, m1, m2) -> bool:
+    return bool(lib().orc_can_merge_same(nb, m1[0], m1[1], m1[2], m2[0], m2[1], m2[2]))
+
+
+def merge_same(nb: int, cost, mi, mj) -> np.ndarray:
+    c = np.ascontiguousarray(cost, np.int64)
+    mi, mj = _i32(mi), _i32(mj)
+    kept = np.zeros(len(c), np.int32)
+    k = lib().orc_merge_same(nb, len(c), _p(c), _p(mi), _p(mj), _p(kept))
+    return kept[:k].copy()
+
+
+def merge_cross(ids, mi, mj, cost) -> np.ndarray:
+    ids, mi, mj = _i32(ids), _i32(mi), _i32(mj)
+    c = np.ascontiguousarray(cost, np.int64)
+    kept = np.zeros(len(c), np.int32)
+    k = lib().orc_merge_cross(len(c), _p(ids), _p(mi), _p(mj), _p(c), _p(kept))
+    return kept[:k].copy()
+
+
+def apply(mid: int, i: int, j: int, tour: np.ndarray) -> None:
+    assert tour.dtype == np.int32 and tour.flags.c_contiguous
+    lib().orc_apply(mid, i, j, len(tour), _p(tour))
+
+
+def pass_(nb: int, tour, D, wide: bool = False, max_moves: int = 1 << 15):
+    t, D = _i32(tour).copy(), _i32(D)
+    ids = np.zeros(max_moves, np.int32)
+    i = np.zeros(max_moves, np.int32)
+    j = np.zeros(max_moves, np.int32)
+    c = np.zeros(max_moves, np.int64)
+    nc = C.c_int64()
+    k = lib().orc_pass(nb, len(t), _p(t), D.shape[0], _p(D), int(wide), max_moves, _p(ids), _p(i), _p(j), _p(c),
+                       C.byref(nc))
+    kk = min(k, max_moves)
+    return t, nc.value, list(zip(ids[:kk].tolist(), i[:kk].tolist(), j[:kk].tolist(), c[:kk].tolist()))
+
+
+def dvnd(tour, D, wide: bool = False, nbs: Sequence[int] = range(5), max_iters: int = 1 << 20,
+         threads: int = 1):
+    t, D = _i32(tour).copy(), _i32(D)
+    nbs_a = _i32(list(nbs))
+    fc, ev, mv = C.c_int64(), C.c_int64(), C.c_int64()
+    it = lib().orc_dvnd(len(t), _p(t), D.shape[0], _p(D), int(wide), len(nbs_a), _p(nbs_a), max_iters, threads,
+                        C.byref(fc), C.byref(ev), C.byref(mv))
+    return t, {"cost": fc.value, "iterations": it, "evals": ev.value, "moves": mv.value}
+
+
+def sweep(tour, D, wide: bool = False, nbs: Sequence[int] = range(5), threads: int = 1):
+    t, D = _i32(tour), _i32(D)
+    nbs_a = _i32(list(nbs))
+    tot = sum(num_blocks(nb, len(t)) for nb in nbs)
+    c = np.zeros(tot, np.int64)
+    i = np.zeros(tot, np.int32)
+    j = np.zeros(tot, np.int32)
+    ev = lib().orc_sweep(len(t), _p(t), D.shape[0], _p(D), int(wide), len(nbs_a), _p(nbs_a), threads, _p(c), _p(i),
+                         _p(j))
+    return int(ev), c, i, j
+
+
+def legacy_no_conflict(m1, m2) -> bool:
+    return bool(lib().orc_legacy_no_conflict(m1[0], m1[1], m1[2], m2[0], m2[1], m2[2]))
+
+
+def legacy_better_no_conflict(moves, maximize: bool = False, melhor_para_pior: bool = False):
+    m = len(moves)
+    ids = _i32([mv[0] for mv in moves])
+    is_ = _i32([mv[1] for mv in moves])
+    js = _i32([mv[2] for mv in moves])
+    cs = _i32([mv[3] for mv in moves])
+    sel = np.zeros(max(m, 1), np.int32)
+    imp = np.zeros(1, np.int32)
+    k = lib().orc_legacy_better_no_conflict(m, _p(ids), _p(is_), _p(js), _p(cs), _p(sel), _p(imp), int(maximize),
+                                            int(melhor_para_pior))
+    return sel[:k].tolist(), int(imp[0]), k
+
+
+def legacy_apply_moves(tour, D, moves):
+    t, D = _i32(tour).copy(), _i32(D)
+    ids = _i32([mv[0] for mv in moves])
+    is_ = _i32([mv[1] for mv in moves])
+    js = _i32([mv[2] for mv in moves])
+    c = lib().orc_legacy_apply_moves(len(t), _p(t), D.shape[0], _p(D), len(moves), _p(ids), _p(is_), _p(js))
+    return t, int(c)
+
+
+# ---------------------------------------------------------------- generators
+def uniform_instance(n: int, seed: int, box: int = 1000):
+    """n points with integer coordinates uniform in [0, box]^2 (seeded)."""
+    r = np.random.default_rng(seed)
+    return r.integers(0, box + 1, n).astype(np.int32), r.integers(0, box + 1, n).astype(np.int32)
+
+
+def clustered_instance(n: int, seed: int, clusters: int = 8, sigma: float = 50.0, box: int = 1000):
+    """n points from `clusters` Gaussian clusters (sigma) with centres uniform in
+    [0, box]^2, rounded and clipped to the box (seeded)."""
+    r = np.random.default_rng(seed)
+    centres = r.uniform(0, box, size=(clusters, 2))
+    lab = r.integers(0, clusters, n)
+    pts = centres[lab] + r.normal(0.0, sigma, size=(n, 2))
+    pts = np.clip(np.rint(pts), 0, box).astype(np.int32)
+    return pts[:, 0].copy(), pts[:, 1].copy()
+
+
+def random_perm_tour(n: int, seed: int) -> np.ndarray:
+    """Depot 0, a seeded random permutation of 1..n-1, depot 0."""
+    r = np.random.default_rng(seed + 1_000_003)
+    return np.concatenate([[0], 1 + r.permutation(n - 1), [0]]).astype(np.int32)

@@ -1,0 +1,202 @@
+"""GPU parity tests: every result of the CUDA path is compared bit-for-bit with
+the oracle (the CPU restatement of the reference) on the same seeded inputs.
+
+Integer/index work, so the bar is exact equality everywhere (no tolerance).
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+BERLIN52 = dict(x=None)
+
+
+def _berlin():
+    import json, os
+    from conftest import GOLDEN
+
+    with open(os.path.join(GOLDEN, "berlin52.json")) as f:
+        g = json.load(f)
+    return np.array(g["x"], np.int32), np.array(g["y"], np.int32), g
+
+
+@pytest.mark.parametrize("n,seed,rnd", [(5, 1, True), (12, 2, False), (52, 3, True), (200, 4, True), (1000, 5, True)])
+def test_dist_matrix(mlpgpu_mod, n, seed, rnd):
+    x, y = oracle.uniform_instance(n, seed)
+    p = mlpgpu_mod.Problem.from_coords(x, y, dist_round=rnd)
+    assert np.array_equal(p.dist(), oracle.dist(x, y, rnd))
+
+
+@pytest.mark.parametrize("n,seed,wide", [(5, 1, False), (6, 7, False), (7, 2, True), (9, 3, False), (13, 4, False),
+                                          (52, 5, False), (101, 6, True), (257, 7, False), (1000, 8, False),
+                                          (1000, 9, True)])
+def test_candidates_all_neighbourhoods(mlpgpu_mod, n, seed, wide):
+    x, y = oracle.uniform_instance(n, seed)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, seed)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True), wide=wide)
+    s.set_tour(t)
+    assert s.cost() == oracle.cost(t, D, wide)
+    assert np.array_equal(s.weights(), oracle.weights(t, D))
+    for nb in range(5):
+        c, i, j = s.eval(nb)
+        oc, oi, oj, _ = oracle.eval_nb(nb, t, D, wide)
+        assert np.array_equal(c, oc), f"nb {nb}: deltas differ"
+        assert np.array_equal(i, oi) and np.array_equal(j, oj), f"nb {nb}: moves differ"
+
+
+@pytest.mark.parametrize("shape", range(6))
+def test_candidates_every_tile_shape(mlpgpu_mod, shape):
+    n = 333
+    x, y = oracle.clustered_instance(n, 11)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, 11)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True))
+    s.set_tile_shape(shape)
+    s.set_tour(t)
+    for nb in range(5):
+        c, i, j = s.eval(nb)
+        oc, oi, oj, _ = oracle.eval_nb(nb, t, D)
+        assert np.array_equal(c, oc) and np.array_equal(i, oi) and np.array_equal(j, oj)
+
+
+def test_k4_berlin52_swap_pass(mlpgpu_mod):
+    """tests/WamcaExperiment.Test.cpp:70-131: random(rng(0), 0.5) then one swap
+    pass (kernel + GPU merge + apply + update) gives 367403."""
+    x, y, g = _berlin()
+    p = mlpgpu_mod.Problem.from_coords(x, y, dist_round=False)
+    D = oracle.dist(x, y, False)
+    t = np.array(g["random_tour_seed0"], np.int32)
+    s = mlpgpu_mod.Solver(p)
+    s.set_tour(t)
+    assert s.cost() == 494309
+    new_cost, moves = s.pass_(0)
+    assert new_cost == 367403
+    ot, oc, omoves = oracle.pass_(0, t, D)
+    assert oc == 367403 and moves == omoves and np.array_equal(s.tour(), ot)
+
+
+@pytest.mark.parametrize("nb", range(5))
+def test_pass_each_neighbourhood(mlpgpu_mod, nb):
+    n = 300
+    x, y = oracle.uniform_instance(n, 20 + nb)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, 20 + nb)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True))
+    s.set_tour(t)
+    new_cost, moves = s.pass_(nb)
+    ot, oc, omoves = oracle.pass_(nb, t, D)
+    assert new_cost == oc
+    assert moves == omoves
+    assert np.array_equal(s.tour(), ot)
+
+
+@pytest.mark.parametrize("n,seed,wide,clustered", [(5, 1, False, False), (8, 2, False, False), (52, 1, False, False),
+                                                   (150, 3, True, True), (400, 4, False, True),
+                                                   (1000, 5, False, False)])
+def test_dvnd_local_optimum(mlpgpu_mod, n, seed, wide, clustered):
+    gen = oracle.clustered_instance if clustered else oracle.uniform_instance
+    x, y = gen(n, seed)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, seed)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True), wide=wide)
+    s.set_tour(t)
+    st = s.dvnd()
+    ot, ost = oracle.dvnd(t, D, wide)
+    assert np.array_equal(s.tour(), ot)
+    assert st["cost"] == ost["cost"] == oracle.cost(ot, D, wide)
+    assert st["iterations"] == ost["iterations"]
+    assert st["moves"] == ost["moves"]
+    assert st["evals"] == ost["evals"]
+    assert st["converged"] == 1
+
+
+def test_dvnd_subset_masks_and_iteration_cap(mlpgpu_mod):
+    n = 250
+    x, y = oracle.uniform_instance(n, 31)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, 31)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True))
+    for nbs in ([0], [1], [2, 3, 4], [0, 2], [1, 4]):
+        mask = sum(1 << q for q in nbs)
+        s.set_tour(t)
+        st = s.dvnd(mask)
+        ot, ost = oracle.dvnd(t, D, nbs=nbs)
+        assert np.array_equal(s.tour(), ot) and st["cost"] == ost["cost"], nbs
+    for cap in (1, 3, 17):
+        s.set_tour(t)
+        st = s.dvnd(max_iters=cap)
+        ot, ost = oracle.dvnd(t, D, max_iters=cap)
+        assert st["sweeps"] == cap
+        assert np.array_equal(s.tour(), ot) and st["cost"] == ost["cost"]
+
+
+def test_ads_buffer_matches_ldsupdate(mlpgpu_mod):
+    x, y, g = _berlin()
+    p = mlpgpu_mod.Problem.from_coords(x, y, dist_round=False)
+    D = oracle.dist(x, y, False)
+    t = np.array(g["random_tour_seed0"], np.int32)
+    s = mlpgpu_mod.Solver(p)
+    s.set_tour(t)
+    a = s.ads()
+    o = oracle.ads(t, D, x, y, False)
+    assert np.array_equal(a, o)
+    ref = np.array(g["ads_random_tour_seed0"], np.uint32)
+    assert np.array_equal(a[:6], ref[:6]) and np.array_equal(a[32:], ref[32:])
+
+
+def test_batch_mixed_sizes_equal_alone(mlpgpu_mod):
+    """Each job of a batch gives exactly the result it gives alone (and the oracle's)."""
+    sizes = [60, 137, 250, 90, 400, 33]
+    b = mlpgpu_mod.Batch()
+    cases = []
+    for q, n in enumerate(sizes):
+        x, y = oracle.clustered_instance(n, 100 + q)
+        D = oracle.dist(x, y, True)
+        t = oracle.random_perm_tour(n, 100 + q)
+        p = mlpgpu_mod.Problem.from_coords(x, y, dist_round=True)
+        b.add(p, t)
+        cases.append((p, D, t))
+    b.run()
+    for q, (p, D, t) in enumerate(cases):
+        bt, bst = b.result(q)
+        ot, ost = oracle.dvnd(t, D)
+        assert np.array_equal(bt, ot) and bst["cost"] == ost["cost"], q
+        s = mlpgpu_mod.Solver(p)
+        s.set_tour(t)
+        s.dvnd()
+        assert np.array_equal(s.tour(), bt)
+    b.reset()
+    b.run()
+    for q, (p, D, t) in enumerate(cases):
+        bt, _ = b.result(q)
+        assert np.array_equal(bt, oracle.dvnd(t, D)[0])
+
+
+def test_matrix_problem_and_errors(mlpgpu_mod):
+    n = 40
+    x, y = oracle.uniform_instance(n, 41)
+    D = oracle.dist(x, y, True)
+    p = mlpgpu_mod.Problem.from_matrix(D)
+    assert np.array_equal(p.dist(), D)
+    s = mlpgpu_mod.Solver(p)
+    t = oracle.random_perm_tour(n, 41)
+    s.set_tour(t)
+    assert np.array_equal(s.tour(), t)
+    bad = t.copy()
+    bad[3] = bad[4]
+    with pytest.raises(mlpgpu_mod.MLPError):
+        s.set_tour(bad)
+    with pytest.raises(mlpgpu_mod.MLPError):
+        s.set_tour(t[:-1])
+    Dbad = D.copy()
+    Dbad[0, 1] += 1
+    with pytest.raises(mlpgpu_mod.MLPError):
+        mlpgpu_mod.Problem.from_matrix(Dbad)
+    with pytest.raises(mlpgpu_mod.MLPError):
+        mlpgpu_mod.Problem.from_coords([0, 1, 2], [0, 1, 2])
+    # the solver still works after rejected calls
+    s.set_tour(t)
+    assert s.dvnd()["cost"] == oracle.dvnd(t, D)[1]["cost"]

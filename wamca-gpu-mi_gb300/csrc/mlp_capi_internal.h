@@ -1,0 +1,37 @@
+// mlp_capi_internal.h -- definitions behind the opaque C-ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "mlp_engine.h"
+
+struct mlp_solver {
+  mlp::Problem* prob = nullptr;
+  bool wide = false;
+  cudaStream_t own_stream = nullptr;
+  std::unique_ptr<mlp::Job> job;
+  std::unique_ptr<mlp::JobSet> set;
+  uint32_t* dads = nullptr;  // reference ADS buffer (allocated on first use)
+  uint32_t* dP = nullptr;    // prefix of T used to write the C matrix
+  ~mlp_solver();
+};
+
+struct mlp_batch {
+  bool wide = false;
+  int shape = -1;
+  int mask = 0x1f;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::vector<std::unique_ptr<mlp::Job>> jobs;
+  std::vector<std::vector<int32_t>> tours;
+  std::unique_ptr<mlp::JobSet> set;
+  ~mlp_batch();
+};
+
+namespace mlp {
+int validate_tour(const int32_t* tour, int len, int n, int size);
+int solver_init(mlp_solver* s, Problem* p, int wide);
+}  // namespace mlp

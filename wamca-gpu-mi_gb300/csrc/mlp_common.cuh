@@ -1,0 +1,216 @@
+// mlp_common.cuh -- shared definitions of the GB300 MLP local-search engine.
+//
+// Position/move conventions follow the reference task API:
+//   size  = tour length = n + 1 (costTour: the tour ends with a copy of depot 0),
+//           source/mlproblem.cpp:68
+//   w[p]  = D[t[p-1]][t[p]] (w[0] = 0), source/mlsolution.cpp:216-228
+//   cost  = sum_{p=1}^{size-1} (size - p) * w[p]
+//   move ids: SWAP 0, 2OPT 1, OROPT-k k+1 (source/mlads.h:26-28, 150-181)
+//
+// Candidate keys.  Each reference "block" of a neighbourhood kernel yields one
+// candidate (source/mlkswap.cu:944-964, mlk2opt.cu:590-611, mlkoropt.cu:742-764).
+// The engine stores it as a 64-bit key ordered by (delta, ctx):
+//   key = (uint64(delta + 2^45) << 14) | ctx          (sweep output)
+// |delta| < 2^45 holds for size <= 16384 and distances <= 65535 (the reference's
+// 14-bit move indices and ushort weights, source/mlads.h:190-195,
+// source/mlsolution.h:79-80).
+#pragma once
+
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define MLP_HD __host__ __device__ __forceinline__
+#else
+#define MLP_HD inline
+#endif
+
+namespace mlp {
+
+constexpr int kNumNb = 5;            // SWAP, 2OPT, OROPT1, OROPT2, OROPT3
+constexpr int kMaxSize = 16384;      // 14-bit i/j in MLMove64
+constexpr int kMaxDist = 65535;      // ushort weights
+constexpr int kCtxBits = 14;
+constexpr uint64_t kCostBias = 1ull << 45;
+constexpr uint64_t kKeyNone = ~0ull;
+constexpr int32_t kCostInfty32 = 0x7fffffff;  // COST_INFTY, source/mlads.h:24
+
+// ---------------- per-neighbourhood candidate layout ----------------
+// Number of reference blocks (= candidates) per neighbourhood for costTour=1.
+MLP_HD int nb_blocks(int nb, int size) {
+  if (nb == 0) return ((size + 1) / 2) - 1;  // mlkswap.cu:1001
+  if (nb == 1) return (size + 1) / 2;        // mlk2opt.cu:680
+  return size - (nb - 1) - 2;                // mlkoropt.cu:842 (tour)
+}
+// ctx range per block (threads that hold a move).
+MLP_HD int nb_threads(int nb, int size) {
+  if (nb == 0) return size - 4;              // mlkswap.cu:763
+  if (nb == 1) return size - 3;              // mlk2opt.cu:559
+  return size - (nb - 1) - 2;                // mlkoropt.cu:699
+}
+MLP_HD int nb_offset(int nb, int size) {
+  int off = 0;
+  for (int q = 0; q < nb; q++) off += nb_blocks(q, size);
+  return off;
+}
+MLP_HD int total_blocks(int size) { return nb_offset(kNumNb, size); }
+
+// (nb, block by, ctx) -> (i, j) of the ODC kernels (costTour = 1).
+MLP_HD void map_move(int nb, int size, int by, int ctx, int& i, int& j) {
+  const bool k = ctx >= by;
+  if (nb == 0) {  // mlkswap.cu:766-768
+    i = k ? by + 1 : size - by - 3;
+    j = k ? ctx + 3 : size - ctx - 2;
+  } else if (nb == 1) {  // mlk2opt.cu:561-563
+    i = k ? ctx - by + 1 : by - ctx;
+    j = k ? ctx + 2 : size - ctx - 2;
+  } else {  // mlkoropt.cu:701-722
+    const int kk = nb - 1;
+    if (k) {
+      i = ctx - by + 1;
+      j = ctx + 2;
+    } else {
+      i = size - ctx - kk - 1;
+      j = by - ctx;
+    }
+  }
+}
+
+MLP_HD uint64_t make_key(int64_t delta, uint32_t low, int low_bits) {
+  return ((uint64_t)(delta + (int64_t)kCostBias) << low_bits) | (uint64_t)low;
+}
+MLP_HD int64_t key_cost(uint64_t key, int low_bits) {
+  return (int64_t)(key >> low_bits) - (int64_t)kCostBias;
+}
+
+// Footprint of a move: the tour positions whose client changes.
+MLP_HD void move_footprint(int id, int i, int j, int& f0, int& f1) {
+  if (id == 0) {
+    f0 = i;
+    f1 = j;
+  } else if (id == 1) {
+    f0 = i;
+    f1 = j;
+  } else {
+    const int k = id - 1;
+    if (i < j) {
+      f0 = i;
+      f1 = j + k - 1;
+    } else {
+      f0 = j;
+      f1 = i + k - 1;
+    }
+  }
+}
+
+// Source position of new position p inside the footprint of a move
+// (the permutation performed by applyMove: mlkswap.cu:1070-1078,
+// mlk2opt.cu:737-745, mlkoropt.cu:896-925).
+MLP_HD int move_source(int id, int i, int j, int p) {
+  if (id == 0) return p == i ? j : (p == j ? i : p);
+  if (id == 1) return i + j - p;
+  const int k = id - 1;
+  if (i < j) return p < j ? p + k : p - j + i;
+  return p < j + k ? p - j + i : p - k;
+}
+
+// ---------------- merge predicates ----------------
+MLP_HD int iabs_(int v) { return v < 0 ? -v : v; }
+MLP_HD int imin_(int a, int b) { return a < b ? a : b; }
+MLP_HD int imax_(int a, int b) { return a > b ? a : b; }
+
+// f_canSwapMerge (mlkernel.cu:51-54)
+MLP_HD bool can_swap_same(int i1, int j1, int i2, int j2) {
+  return iabs_(i1 - i2) > 1 && iabs_(i1 - j2) > 1 && iabs_(j1 - i2) > 1 && iabs_(j1 - j2) > 1;
+}
+// f_can2OptMerge (mlkernel.cu:56-59)
+MLP_HD bool can_2opt_same(int i1, int j1, int i2, int j2) {
+  return (j1 < i2 - 1) || (i1 > j2 + 1) || (j2 < i1 - 1) || (i2 > j1 + 1);
+}
+// f_canOrOptMerge (mlkernel.cu:61-71)
+MLP_HD bool can_oropt_same(int id1, int i1, int j1, int id2, int i2, int j2) {
+  return (imax_(i1, j1) + (id1 - 1) < imin_(i2, j2)) || (imin_(i1, j1) > imax_(i2, j2) + (id2 - 1));
+}
+// canSwapMerge / can2OptMerge / canOrOptMerge / canMerge (mlkernel.cu:649-729)
+MLP_HD bool can_merge_swap(int i1, int j1, int id2, int i2, int j2) {
+  if (id2 == 0) return can_swap_same(i1, j1, i2, j2);
+  if (id2 == 1) return ((i1 < i2 - 1) || (i1 > j2 + 1)) && ((j1 < i2 - 1) || (j1 > j2 + 1));
+  const int mn = imin_(i2, j2), mx = imax_(i2, j2), k2 = id2 - 1;
+  return (j1 < mn - 1) || (i1 > mx + k2) || ((i1 < mn - 1) && (j1 > mx + k2));
+}
+MLP_HD bool can_merge_2opt(int i1, int j1, int id2, int i2, int j2) {
+  if (id2 == 0) return can_merge_swap(i2, j2, 1, i1, j1);
+  if (id2 == 1) return can_2opt_same(i1, j1, i2, j2);
+  const int mn = imin_(i2, j2), mx = imax_(i2, j2), k2 = id2 - 1;
+  return (i1 > mx + k2) || (j1 < mn - 1);
+}
+MLP_HD bool can_merge(int id1, int i1, int j1, int id2, int i2, int j2) {
+  if (id1 == 0) return can_merge_swap(i1, j1, id2, i2, j2);
+  if (id1 == 1) return can_merge_2opt(i1, j1, id2, i2, j2);
+  if (id2 == 0) return can_merge_swap(i2, j2, id1, i1, j1);
+  if (id2 == 1) return can_merge_2opt(i2, j2, id1, i1, j1);
+  return can_oropt_same(id1, i1, j1, id2, i2, j2);
+}
+
+// Conflict interval of a same-neighbourhood interval move: two moves of
+// neighbourhood nb (2OPT or OROPT-k) conflict iff their closed intervals
+// intersect.  2OPT: f_can2OptMerge <=> [i1, j1+1] and [i2, j2+1] disjoint.
+// OROPT-k: f_canOrOptMerge <=> [min, max+k] disjoint.
+MLP_HD void conflict_interval(int id, int i, int j, int& a, int& b) {
+  if (id == 1) {
+    a = i;
+    b = j + 1;
+  } else {
+    a = imin_(i, j);
+    b = imax_(i, j) + (id - 1);
+  }
+}
+
+// ---------------- device job descriptor ----------------
+// All pointers are device pointers.  Arrays of per-position data are padded
+// to size + 8 entries (zero beyond size - 1).
+struct JobDev {
+  const int32_t* D;   // n x n distances (node ids)
+  int32_t* tour;      // size
+  int32_t* tour_alt;  // size (apply double buffer)
+  int32_t* w;         // size + 8
+  void* W;            // prefix of w: uint32 (int32 mode) or int64 (wide)
+  void* Q;            // prefix of p * w[p]
+  int32_t* A;         // 3 x (size + 8): A[k-1][p] = D[t[p-1]][t[p+k]]
+  uint64_t* keys;     // total_blocks(size) candidate keys
+  uint64_t* kept;     // total_blocks(size) stage-2 kept entries (packed)
+  int32_t* kept_count;  // kNumNb counters
+  uint8_t* ws;        // global workspace for large sizes (may be null)
+  int64_t* stats;     // kStat* words
+  uint32_t* moves_out;  // optional: applied moves (id | i << 4 | j << 18)
+  int64_t* moves_cost;  // optional: applied move deltas
+  int32_t moves_cap;
+  int32_t n;
+  int32_t size;
+  int32_t nb_mask;    // neighbourhoods evaluated and merged
+  int32_t flags;
+};
+
+enum : int {
+  kStatCost = 0,       // current cost (int64, or uint32 zero-extended)
+  kStatIters = 1,      // iterations that applied moves
+  kStatMoves = 2,      // moves applied (total)
+  kStatConverged = 3,  // 1 once an iteration found no improving candidate
+  kStatLastMoves = 4,  // moves applied by the last iteration
+  kStatDone = 5,       // stage-2 CTA arrival counter
+  kStatSweeps = 6,     // sweeps run
+  kStatError = 7,      // nonzero: device-detected error
+  kStatLimit = 8,      // sweeps allowed (kernels become no-ops past it)
+  kStatWords = 16
+};
+
+enum : int { kFlagWide = 1 };
+
+// Sweep work item: one parallelogram tile of the (row r, diagonal L) plane.
+struct SweepTile {
+  int32_t job;
+  int32_t r0;
+  int32_t L0;
+  int32_t pad;
+};
+
+}  // namespace mlp

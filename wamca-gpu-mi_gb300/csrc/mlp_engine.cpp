@@ -1,0 +1,491 @@
+// mlp_engine.cpp -- host side of the GB300 MLP local-search engine.
+#include "mlp_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "mlp_kernels.cuh"
+
+namespace mlp {
+
+namespace {
+thread_local std::string g_last_error;
+
+size_t al(size_t v) { return (v + 255) / 256 * 256; }
+}  // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error() { return g_last_error.c_str(); }
+
+int cuda_status(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return kOk;
+  set_error(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+  return e == cudaErrorMemoryAllocation ? kErrNoMem : kErrCuda;
+}
+
+#define MLP_CUDA(call, what)                        \
+  do {                                              \
+    int st_ = cuda_status((call), what);            \
+    if (st_ != kOk) return st_;                     \
+  } while (0)
+
+// ---------------------------------------------------------------- Problem
+Problem::~Problem() {
+  if (dD) cudaFree(dD);
+  if (dX) cudaFree(dX);
+  if (dY) cudaFree(dY);
+}
+
+static int check_n(int n, int cost_tour) {
+  if (cost_tour != 1) {
+    set_error("only costTour = 1 (closed tour with the depot repeated at the end) is supported; "
+              "the reference's Or-opt kernels read past the tour for paths");
+    return kErrUnsupported;
+  }
+  if (n < 5 || n + 1 > kMaxSize) {
+    set_error("instance size out of range: need 5 <= n and n + 1 <= 16384 (14-bit move indices)");
+    return kErrRange;
+  }
+  return kOk;
+}
+
+int problem_from_coords(int n, const int32_t* x, const int32_t* y, int cost_tour, int dist_round,
+                        bool on_device, Problem** out) {
+  if (!x || !y || !out) {
+    set_error("null argument");
+    return kErrArg;
+  }
+  int st = check_n(n, cost_tour);
+  if (st != kOk) return st;
+  std::unique_ptr<Problem> p(new Problem());
+  p->n = n;
+  p->size = n + cost_tour;
+  p->cost_tour = cost_tour;
+  p->dist_round = dist_round ? 1 : 0;
+  MLP_CUDA(cudaGetDevice(&p->device), "cudaGetDevice");
+  MLP_CUDA(cudaMalloc(&p->dX, sizeof(int32_t) * n), "cudaMalloc(coords)");
+  MLP_CUDA(cudaMalloc(&p->dY, sizeof(int32_t) * n), "cudaMalloc(coords)");
+  MLP_CUDA(cudaMalloc(&p->dD, sizeof(int32_t) * (size_t)n * n + 16), "cudaMalloc(D)");
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  MLP_CUDA(cudaMemcpy(p->dX, x, sizeof(int32_t) * n, kind), "copy coords");
+  MLP_CUDA(cudaMemcpy(p->dY, y, sizeof(int32_t) * n, kind), "copy coords");
+  p->hx.resize(n);
+  p->hy.resize(n);
+  MLP_CUDA(cudaMemcpy(p->hx.data(), p->dX, sizeof(int32_t) * n, cudaMemcpyDeviceToHost), "copy coords");
+  MLP_CUDA(cudaMemcpy(p->hy.data(), p->dY, sizeof(int32_t) * n, cudaMemcpyDeviceToHost), "copy coords");
+  {
+    const auto mmx = std::minmax_element(p->hx.begin(), p->hx.end());
+    const auto mmy = std::minmax_element(p->hy.begin(), p->hy.end());
+    if ((int64_t)*mmx.second - *mmx.first > 32767 || (int64_t)*mmy.second - *mmy.first > 32767) {
+      set_error("coordinate spans must not exceed 32767 so that dx*dx + dy*dy fits int32");
+      return kErrRange;
+    }
+  }
+  int32_t* dmax = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(p->dD) + sizeof(int32_t) * (size_t)n * n);
+  MLP_CUDA(cudaMemset(dmax, 0, sizeof(int32_t)), "memset");
+  MLP_CUDA(launch_dist(p->dX, p->dY, n, p->dist_round, p->dD, dmax, 0), "dist kernel");
+  MLP_CUDA(cudaMemcpy(&p->dmax, dmax, sizeof(int32_t), cudaMemcpyDeviceToHost), "dist kernel");
+  if (p->dmax > kMaxDist) {
+    set_error("a distance exceeds 65535 (the reference stores weights as ushort)");
+    return kErrRange;
+  }
+  *out = p.release();
+  return kOk;
+}
+
+int problem_from_matrix(int n, const int32_t* D, int cost_tour, bool on_device, Problem** out) {
+  if (!D || !out) {
+    set_error("null argument");
+    return kErrArg;
+  }
+  int st = check_n(n, cost_tour);
+  if (st != kOk) return st;
+  std::vector<int32_t> h;
+  const int32_t* hd = D;
+  if (on_device) {
+    h.resize((size_t)n * n);
+    MLP_CUDA(cudaMemcpy(h.data(), D, sizeof(int32_t) * (size_t)n * n, cudaMemcpyDeviceToHost), "copy D");
+    hd = h.data();
+  }
+  int32_t mx = 0;
+  for (int i = 0; i < n; i++) {
+    for (int j = 0; j < n; j++) {
+      const int32_t v = hd[(size_t)i * n + j];
+      if (v < 0 || v > kMaxDist) {
+        set_error("distances must lie in [0, 65535] (the reference stores weights as ushort)");
+        return kErrRange;
+      }
+      if (v != hd[(size_t)j * n + i]) {
+        set_error("the distance matrix must be symmetric (the move deltas assume d(a,b) = d(b,a))");
+        return kErrArg;
+      }
+      mx = std::max(mx, v);
+    }
+  }
+  std::unique_ptr<Problem> p(new Problem());
+  p->n = n;
+  p->size = n + cost_tour;
+  p->cost_tour = cost_tour;
+  p->dmax = mx;
+  MLP_CUDA(cudaGetDevice(&p->device), "cudaGetDevice");
+  MLP_CUDA(cudaMalloc(&p->dD, sizeof(int32_t) * (size_t)n * n + 16), "cudaMalloc(D)");
+  MLP_CUDA(cudaMemcpy(p->dD, hd, sizeof(int32_t) * (size_t)n * n, cudaMemcpyHostToDevice), "copy D");
+  *out = p.release();
+  return kOk;
+}
+
+// TSPLIB header + NODE_COORD_SECTION reader; coordinates are read as float and
+// rounded with nint (TSPLibInstance::inear, source/tsplib.cpp:237-240), as
+// MLProblem::load does (source/mlproblem.cpp:116-117).
+int read_tsplib_euc2d(const char* path, std::vector<int32_t>& x, std::vector<int32_t>& y,
+                      std::string& name) {
+  std::ifstream f(path);
+  if (!f.is_open()) {
+    set_error(std::string("cannot open instance file: ") + (path ? path : "(null)"));
+    return kErrIo;
+  }
+  auto trim = [](const std::string& s) {
+    size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+  };
+  std::string line;
+  int dim = -1;
+  std::string ewt;
+  bool coords = false;
+  while (std::getline(f, line)) {
+    size_t c = line.find(':');
+    std::string key = trim(c == std::string::npos ? line : line.substr(0, c));
+    std::string val = c == std::string::npos ? std::string() : trim(line.substr(c + 1));
+    if (key == "NAME") name = val;
+    else if (key == "DIMENSION") dim = std::atoi(val.c_str());
+    else if (key == "EDGE_WEIGHT_TYPE") ewt = val;
+    else if (key == "NODE_COORD_SECTION") {
+      coords = true;
+      break;
+    }
+  }
+  if (ewt != "EUC_2D") {
+    set_error("invalid instance: only EUC_2D coordinates are supported (source/mlproblem.cpp:94-95)");
+    return kErrFormat;
+  }
+  if (!coords || dim <= 0) {
+    set_error("invalid instance: missing DIMENSION or NODE_COORD_SECTION");
+    return kErrFormat;
+  }
+  x.resize(dim);
+  y.resize(dim);
+  for (int i = 0; i < dim; i++) {
+    int id;
+    float fx, fy;
+    if (!(f >> id >> fx >> fy)) {
+      set_error("invalid instance: truncated NODE_COORD_SECTION");
+      return kErrFormat;
+    }
+    x[i] = fx >= 0 ? (int)(fx + 0.5F) : (int)(fx - 0.5F);
+    y[i] = fy >= 0 ? (int)(fy + 0.5F) : (int)(fy - 0.5F);
+  }
+  return kOk;
+}
+
+int problem_from_tsplib(const char* path, int cost_tour, int dist_round, Problem** out) {
+  std::vector<int32_t> x, y;
+  std::string name;
+  int st = read_tsplib_euc2d(path, x, y, name);
+  if (st != kOk) return st;
+  st = problem_from_coords((int)x.size(), x.data(), y.data(), cost_tour, dist_round, false, out);
+  if (st == kOk) (*out)->name = name;
+  return st;
+}
+
+// ---------------------------------------------------------------- Job
+size_t job_bytes(int size, bool wide, int moves_cap) {
+  const size_t pad = size + 8, tb = total_blocks(size), cw = wide ? 8 : 4;
+  size_t b = 0;
+  b += al(4 * (size_t)size) * 2;        // tour, tour_alt
+  b += al(4 * pad);                     // w
+  b += al(cw * pad) * 2;                // W, Q
+  b += al(4 * 3 * pad);                 // A
+  b += al(8 * tb);                      // keys
+  b += al(16 * tb);                     // kept
+  b += al(4 * 8);                       // kept_count
+  b += al(8 * kStatWords);              // stats
+  b += al(4 * (size_t)moves_cap) + al(8 * (size_t)moves_cap);
+  if (size > merge_smem_max_size()) b += al(merge_ws_bytes(size));
+  return b;
+}
+
+Job::~Job() {
+  if (arena) cudaFree(arena);
+}
+
+int job_create(Problem* p, bool wide, int moves_cap, Job** out) {
+  std::unique_ptr<Job> j(new Job());
+  j->prob = p;
+  j->wide = wide;
+  j->size = p->size;
+  j->moves_cap = moves_cap;
+  const int size = p->size;
+  const size_t pad = size + 8, tb = total_blocks(size), cw = wide ? 8 : 4;
+  j->arena_bytes = job_bytes(size, wide, moves_cap);
+  MLP_CUDA(cudaMalloc(&j->arena, j->arena_bytes), "cudaMalloc(job)");
+  MLP_CUDA(cudaMemset(j->arena, 0, j->arena_bytes), "memset(job)");
+  char* c = static_cast<char*>(j->arena);
+  JobDev& d = j->dev;
+  d.D = p->dD;
+  d.tour = (int32_t*)c;  c += al(4 * (size_t)size);
+  d.tour_alt = (int32_t*)c;  c += al(4 * (size_t)size);
+  d.w = (int32_t*)c;  c += al(4 * pad);
+  d.W = c;  c += al(cw * pad);
+  d.Q = c;  c += al(cw * pad);
+  d.A = (int32_t*)c;  c += al(4 * 3 * pad);
+  d.keys = (uint64_t*)c;  c += al(8 * tb);
+  d.kept = (uint64_t*)c;  c += al(16 * tb);
+  d.kept_count = (int32_t*)c;  c += al(4 * 8);
+  d.stats = (int64_t*)c;  c += al(8 * kStatWords);
+  d.moves_out = moves_cap > 0 ? (uint32_t*)c : nullptr;  c += al(4 * (size_t)moves_cap);
+  d.moves_cost = moves_cap > 0 ? (int64_t*)c : nullptr;  c += al(8 * (size_t)moves_cap);
+  d.ws = nullptr;
+  if (size > merge_smem_max_size()) {
+    d.ws = (uint8_t*)c;
+    c += al(merge_ws_bytes(size));
+  }
+  d.moves_cap = moves_cap;
+  d.n = p->n;
+  d.size = size;
+  d.nb_mask = 0x1f;
+  d.flags = wide ? kFlagWide : 0;
+  *out = j.release();
+  return kOk;
+}
+
+int default_shape(int size) {
+  if (size <= 320) return 0;    // 32 x 16
+  if (size <= 1400) return 2;   // 64 x 16
+  return 5;                     // 128 x 32
+}
+
+// ---------------------------------------------------------------- JobSet
+JobSet::JobSet(std::vector<Job*> jobs, bool wide, cudaStream_t stream)
+    : jobs_(std::move(jobs)), wide_(wide), stream_(stream) {}
+
+JobSet::~JobSet() {
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  if (djobs_) cudaFree(djobs_);
+  if (dtiles_) cudaFree(dtiles_);
+  if (hstats_) cudaFreeHost(hstats_);
+  if (dstats_) cudaFree(dstats_);
+}
+
+int JobSet::init() {
+  if (jobs_.empty()) {
+    set_error("empty job set");
+    return kErrArg;
+  }
+  max_size_ = 0;
+  for (Job* j : jobs_) {
+    if (j->wide != wide_) {
+      set_error("all jobs of a set must share the cost width");
+      return kErrArg;
+    }
+    max_size_ = std::max(max_size_, j->size);
+  }
+  merge_smem_ = max_size_ <= merge_smem_max_size();
+  if (!merge_smem_) {
+    for (Job* j : jobs_)
+      if (j->dev.ws == nullptr) {
+        set_error("a job set mixing sizes above and below 2044 needs every job sized above it");
+        return kErrUnsupported;
+      }
+  }
+  if (merge_smem_) MLP_CUDA(configure_merge(merge_smem_bytes(max_size_)), "configure merge");
+  MLP_CUDA(cudaMallocHost(&hstats_, sizeof(int64_t) * kStatWords * jobs_.size()), "cudaMallocHost");
+  MLP_CUDA(cudaMalloc(&dstats_, sizeof(int64_t) * kStatWords * jobs_.size()), "cudaMalloc(stats)");
+  MLP_CUDA(cudaMemset(dstats_, 0, sizeof(int64_t) * kStatWords * jobs_.size()), "memset(stats)");
+  MLP_CUDA(cudaMalloc(&djobs_, sizeof(JobDev) * jobs_.size()), "cudaMalloc(jobs)");
+  std::vector<JobDev> h(jobs_.size());
+  for (size_t q = 0; q < jobs_.size(); q++) {
+    jobs_[q]->dev.stats = dstats_ + q * kStatWords;
+    h[q] = jobs_[q]->dev;
+  }
+  MLP_CUDA(cudaMemcpy(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice), "copy jobs");
+  if (shape_ < 0) shape_ = default_shape(max_size_);
+  return build_tiles();
+}
+
+int JobSet::build_tiles() {
+  const TileShape ts = kTileShapes[shape_];
+  std::vector<SweepTile> tiles;
+  for (size_t q = 0; q < jobs_.size(); q++) {
+    const int sz = jobs_[q]->size;
+    for (int r0 = 1; r0 <= sz - 3; r0 += ts.tr)
+      for (int L0 = 1; r0 + L0 <= sz - 2; L0 += ts.tl) tiles.push_back(SweepTile{(int32_t)q, r0, L0, 0});
+  }
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+  if (dtiles_) cudaFree(dtiles_);
+  dtiles_ = nullptr;
+  ntiles_ = (int)tiles.size();
+  MLP_CUDA(cudaMalloc(&dtiles_, sizeof(SweepTile) * std::max<size_t>(1, tiles.size())), "cudaMalloc(tiles)");
+  MLP_CUDA(cudaMemcpy(dtiles_, tiles.data(), sizeof(SweepTile) * tiles.size(), cudaMemcpyHostToDevice),
+           "copy tiles");
+  return kOk;
+}
+
+int JobSet::set_stream(cudaStream_t s) {
+  stream_ = s;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+  return kOk;
+}
+
+int JobSet::set_shape(int shape) {
+  if (shape < 0 || shape >= kNumTileShapes) {
+    set_error("tile shape index out of range");
+    return kErrArg;
+  }
+  shape_ = shape;
+  return djobs_ ? build_tiles() : kOk;
+}
+
+int JobSet::set_unroll(int u) {
+  if (u < 1 || u > 256) {
+    set_error("unroll out of range [1, 256]");
+    return kErrArg;
+  }
+  unroll_ = u;
+  return kOk;
+}
+
+int JobSet::set_mask(int mask) {
+  if (mask <= 0 || mask > 0x1f) {
+    set_error("neighbourhood mask must be a nonzero subset of 0x1f");
+    return kErrArg;
+  }
+  if (mask == mask_) return kOk;
+  mask_ = mask;
+  for (size_t q = 0; q < jobs_.size(); q++) {
+    jobs_[q]->dev.nb_mask = mask;
+    MLP_CUDA(cudaMemcpyAsync(&djobs_[q].nb_mask, &jobs_[q]->dev.nb_mask, sizeof(int32_t),
+                             cudaMemcpyHostToDevice, stream_),
+             "set mask");
+  }
+  MLP_CUDA(cudaStreamSynchronize(stream_), "set mask");
+  return kOk;
+}
+
+int JobSet::prepare(bool reset_stats) {
+  MLP_CUDA(launch_prepare(djobs_, (int)jobs_.size(), wide_, reset_stats, stream_), "prepare kernel");
+  return kOk;
+}
+
+int JobSet::launch_iteration() {
+  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
+  MLP_CUDA(launch_merge(djobs_, (int)jobs_.size(), wide_, merge_smem_, max_size_, stream_), "merge kernel");
+  return kOk;
+}
+
+int JobSet::sweep_only() {
+  MLP_CUDA(launch_stats_begin(djobs_, (int)jobs_.size(), 1, stream_), "stats kernel");
+  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
+  return kOk;
+}
+
+int JobSet::graph_for(int iters, cudaGraphExec_t* out) {
+  auto it = graphs_.find(iters);
+  if (it != graphs_.end()) {
+    *out = it->second;
+    return kOk;
+  }
+  cudaGraph_t g;
+  MLP_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
+  for (int q = 0; q < iters; q++) {
+    int st = launch_iteration();
+    if (st != kOk) {
+      cudaStreamEndCapture(stream_, &g);
+      return st;
+    }
+  }
+  MLP_CUDA(cudaStreamEndCapture(stream_, &g), "end capture");
+  cudaGraphExec_t ge;
+  cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  MLP_CUDA(e, "graph instantiate");
+  graphs_[iters] = ge;
+  *out = ge;
+  return kOk;
+}
+
+int JobSet::enqueue_iterations(int iters) {
+  if (stream_ == 0) {
+    for (int q = 0; q < iters; q++) {
+      int st = launch_iteration();
+      if (st != kOk) return st;
+    }
+    return kOk;
+  }
+  while (iters > 0) {
+    const int u = std::min(iters, unroll_);
+    cudaGraphExec_t ge;
+    int st = graph_for(u, &ge);
+    if (st != kOk) return st;
+    MLP_CUDA(cudaGraphLaunch(ge, stream_), "graph launch");
+    iters -= u;
+  }
+  return kOk;
+}
+
+int JobSet::run(int max_iters, bool sync) {
+  if (max_iters <= 0) {
+    set_error("max_iters must be positive");
+    return kErrArg;
+  }
+  MLP_CUDA(launch_stats_begin(djobs_, (int)jobs_.size(), max_iters, stream_), "stats kernel");
+  int done = 0;
+  while (done < max_iters) {
+    const int u = std::min(unroll_, max_iters - done);
+    int st = enqueue_iterations(u);
+    if (st != kOk) return st;
+    done += u;
+    if (!sync && done < max_iters) continue;
+    std::vector<std::array<int64_t, kStatWords>> s;
+    st = read_stats(&s);
+    if (st != kOk) return st;
+    bool all = true;
+    for (auto& a : s)
+      if (!a[kStatConverged] && a[kStatSweeps] < max_iters) all = false;
+    if (all) break;
+  }
+  return kOk;
+}
+
+int JobSet::read_stats(std::vector<std::array<int64_t, kStatWords>>* out) {
+  MLP_CUDA(cudaMemcpyAsync(hstats_, dstats_, sizeof(int64_t) * kStatWords * jobs_.size(),
+                           cudaMemcpyDeviceToHost, stream_),
+           "read stats");
+  MLP_CUDA(cudaStreamSynchronize(stream_), "read stats");
+  out->resize(jobs_.size());
+  for (size_t q = 0; q < jobs_.size(); q++)
+    std::memcpy((*out)[q].data(), hstats_ + q * kStatWords, sizeof(int64_t) * kStatWords);
+  int64_t err = 0;
+  for (auto& a : *out) err |= a[kStatError];
+  if (err) {
+    set_error("device reported an internal error");
+    return kErrState;
+  }
+  return kOk;
+}
+
+int64_t JobSet::evals_per_sweep(int job, int mask) const {
+  const int sz = jobs_[job]->size;
+  int64_t e = 0;
+  for (int nb = 0; nb < kNumNb; nb++)
+    if ((mask >> nb) & 1) e += (int64_t)nb_blocks(nb, sz) * nb_threads(nb, sz);
+  return e;
+}
+
+}  // namespace mlp

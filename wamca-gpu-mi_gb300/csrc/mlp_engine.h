@@ -1,0 +1,140 @@
+// mlp_engine.h -- host side of the GB300 MLP local-search engine (internal C++).
+//
+// The reference's task objects map onto this engine as follows:
+//   MLProblem   (source/mlproblem.h:61-151)   -> mlp::Problem: n x n int32 distance
+//               matrix resident in HBM, built on the device from coordinates or
+//               uploaded from the host.
+//   MLSolution  (source/mlsolution.h:62-434)  -> the tour + ADS prefix arrays of a Job.
+//   MLKernel*   (source/mlkernel.h:104-318)   -> mlp::JobSet: the fused sweep over the
+//               five neighbourhoods, the device merge/apply and the ADS rebuild,
+//               launched on one stream and captured into CUDA graphs.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mlp_common.cuh"
+
+namespace mlp {
+
+// Status codes of the C-ABI (mirrored in include/mlp_gpu.h).
+enum Status : int {
+  kOk = 0,
+  kErrArg = 1,
+  kErrCuda = 2,
+  kErrRange = 3,
+  kErrIo = 4,
+  kErrFormat = 5,
+  kErrNoMem = 6,
+  kErrState = 7,
+  kErrUnsupported = 8,
+};
+
+void set_error(const std::string& msg);
+const char* last_error();
+int cuda_status(cudaError_t e, const char* what);
+
+struct Problem {
+  int n = 0;
+  int size = 0;
+  int cost_tour = 1;
+  int dist_round = 0;
+  int device = 0;
+  int32_t dmax = 0;
+  int32_t* dD = nullptr;  // n x n
+  int32_t* dX = nullptr;  // node coordinates (optional)
+  int32_t* dY = nullptr;
+  std::vector<int32_t> hx, hy;
+  std::string name;
+  ~Problem();
+};
+
+int problem_from_coords(int n, const int32_t* x, const int32_t* y, int cost_tour, int dist_round,
+                        bool x_on_device, Problem** out);
+int problem_from_matrix(int n, const int32_t* D, int cost_tour, bool on_device, Problem** out);
+int problem_from_tsplib(const char* path, int cost_tour, int dist_round, Problem** out);
+// TSPLIB EUC_2D reader (coordinates rounded with TSPLIB nint, source/tsplib.cpp:237-240).
+int read_tsplib_euc2d(const char* path, std::vector<int32_t>& x, std::vector<int32_t>& y,
+                      std::string& name);
+
+// One local-search job: a problem plus its device-resident tour and ADS arrays.
+struct Job {
+  Problem* prob = nullptr;
+  bool wide = false;
+  int size = 0;
+  void* arena = nullptr;  // single device allocation holding every array
+  size_t arena_bytes = 0;
+  JobDev dev{};           // host copy of the descriptor
+  int moves_cap = 0;
+  ~Job();
+};
+
+int job_create(Problem* p, bool wide, int moves_cap, Job** out);
+size_t job_bytes(int size, bool wide, int moves_cap);
+
+struct DvndResult {
+  int64_t cost = 0;
+  int64_t iterations = 0;   // iterations that applied moves
+  int64_t sweeps = 0;       // neighbourhood sweeps run
+  int64_t moves = 0;        // moves applied
+  int64_t evals = 0;        // move evaluations
+  int converged = 0;
+};
+
+// A set of jobs processed by the same launches (one job for the plain form,
+// many for the batched form).
+class JobSet {
+ public:
+  JobSet(std::vector<Job*> jobs, bool wide, cudaStream_t stream);
+  ~JobSet();
+  int init();
+  int set_stream(cudaStream_t s);
+  cudaStream_t stream() const { return stream_; }
+  int set_shape(int shape);
+  int shape() const { return shape_; }
+  int set_unroll(int u);
+  // Rebuild the ADS arrays and reset statistics (after new tours).
+  int prepare(bool reset_stats);
+  // Set the neighbourhood mask of every job (bit nb = neighbourhood nb).
+  int set_mask(int mask);
+  // One sweep only (keys left on the device; call prepare() afterwards).
+  int sweep_only();
+  // DVND iterations until every job converged or max_iters sweeps ran.
+  int run(int max_iters, bool sync);
+  // Enqueue `iters` iterations without host synchronisation (graph replay).
+  int enqueue_iterations(int iters);
+  int read_stats(std::vector<std::array<int64_t, kStatWords>>* out);
+  int64_t evals_per_sweep(int job, int mask) const;
+  const std::vector<Job*>& jobs() const { return jobs_; }
+  JobDev* device_jobs() const { return djobs_; }
+  int ntiles() const { return ntiles_; }
+
+ private:
+  int build_tiles();
+  int graph_for(int iters, cudaGraphExec_t* out);
+  int launch_iteration();
+  std::vector<Job*> jobs_;
+  bool wide_;
+  cudaStream_t stream_;
+  int shape_ = -1;
+  int unroll_ = 16;
+  int mask_ = 0x1f;
+  int max_size_ = 0;
+  bool merge_smem_ = true;
+  JobDev* djobs_ = nullptr;
+  SweepTile* dtiles_ = nullptr;
+  int ntiles_ = 0;
+  int64_t* hstats_ = nullptr;  // pinned, kStatWords per job
+  int64_t* dstats_ = nullptr;  // device, kStatWords per job (jobs' stats live here)
+  std::map<int, cudaGraphExec_t> graphs_;
+};
+
+int default_shape(int size);
+
+}  // namespace mlp

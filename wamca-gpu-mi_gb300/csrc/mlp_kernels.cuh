@@ -1,0 +1,48 @@
+// mlp_kernels.cuh -- launch entry points of the engine's CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mlp_common.cuh"
+
+namespace mlp {
+
+// Sweep tile shapes (diagonals x rows) compiled into the library.
+struct TileShape {
+  int tl;  // diagonals per tile (= threads per CTA)
+  int tr;  // rows per tile
+};
+constexpr TileShape kTileShapes[] = {{32, 16}, {64, 8}, {64, 16}, {64, 32}, {128, 16}, {128, 32}};
+constexpr int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
+
+// Bytes of dynamic shared memory the merge kernel needs for `size`
+// (0 if the job must use its global workspace instead).
+size_t merge_smem_bytes(int size);
+// Bytes of global workspace a job of `size` needs when the merge cannot run
+// from shared memory.
+size_t merge_ws_bytes(int size);
+// Largest size whose merge workspace fits in shared memory.
+int merge_smem_max_size();
+
+// Opt the merge kernels into `bytes` of dynamic shared memory (call before
+// launching or capturing merges that use shared memory).
+cudaError_t configure_merge(size_t bytes);
+// Zero the run counters of every job and set its sweep limit.
+cudaError_t launch_stats_begin(const JobDev* jobs, int njobs, int64_t limit, cudaStream_t s);
+cudaError_t launch_prepare(const JobDev* jobs, int njobs, bool wide, bool reset_stats,
+                           cudaStream_t s);
+cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
+                         int shape, cudaStream_t s);
+cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
+                         cudaStream_t s);
+// Reference ADS buffer (source/mlads.h:38-74) of each job's current tour.
+cudaError_t launch_ads(const JobDev* job, const int32_t* cx, const int32_t* cy, uint32_t* ads,
+                       int cost_tour, int dist_round, cudaStream_t s, uint32_t* Pbuf, int size);
+// D[a][b] = int(sqrtf(float(dx^2 + dy^2)) + dr)  (source/mlproblem.cpp:153-166)
+cudaError_t launch_dist(const int32_t* x, const int32_t* y, int n, int dist_round, int32_t* D,
+                        int32_t* dmax, cudaStream_t s);
+// Sequential application of legacy moves (source/dvnd.cpp:16-145).
+// `moves` holds m (id, i, j) int32 triples.
+cudaError_t launch_legacy_apply(const JobDev* job, const int32_t* moves, int m, cudaStream_t s);
+
+}  // namespace mlp

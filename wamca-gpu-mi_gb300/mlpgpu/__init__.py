@@ -1,0 +1,407 @@
+"""Python host binding of libmlpgpu.so (the GB300 MLP local-search engine).
+
+A thin ctypes layer over the C-ABI of include/mlp_gpu.h and
+include/wamca_dvnd.h, shaped like the reference's task API:
+
+    MLProblem  -> Problem   (source/mlproblem.h:61-151)
+    MLSolution + MLKernel{Swap,2Opt,OrOpt}
+               -> Solver    (source/mlsolution.h:62-434, source/mlkernel.h:104-318)
+    legacy extern "C" DVND entry points -> Legacy (source/dvnd.cuh, source/dvnd.h)
+
+There is no CPU fallback: every call goes to the CUDA library, and importing
+this module fails loudly if the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libmlpgpu.so")
+
+NB_SWAP, NB_2OPT, NB_OROPT1, NB_OROPT2, NB_OROPT3 = range(5)
+NB_ALL = 0x1F
+NB_NAMES = ("swap", "2opt", "oropt1", "oropt2", "oropt3")
+
+
+class MLPError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class DvndStats(C.Structure):
+    _fields_ = [
+        ("cost", C.c_int64),
+        ("iterations", C.c_int64),
+        ("sweeps", C.c_int64),
+        ("moves", C.c_int64),
+        ("evals", C.c_int64),
+        ("converged", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_ if f != "reserved"}
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def lib() -> C.CDLL:
+    """Loads libmlpgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() "
+                          "or python wamca-gpu-mi_gb300/build_lib.py")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, u32 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32
+    P = C.POINTER
+    sig = {
+        "mlp_version": (C.c_int, []),
+        "mlp_last_error": (C.c_char_p, []),
+        "mlp_status_string": (C.c_char_p, [C.c_int]),
+        "mlp_device_count": (C.c_int, [P(i32)]),
+        "mlp_set_device": (C.c_int, [i32]),
+        "mlp_problem_create_coords": (C.c_int, [i32, vp, vp, i32, i32, P(vp)]),
+        "mlp_problem_create_coords_device": (C.c_int, [i32, vp, vp, i32, i32, P(vp)]),
+        "mlp_problem_create_matrix": (C.c_int, [i32, vp, i32, P(vp)]),
+        "mlp_problem_load_tsplib": (C.c_int, [C.c_char_p, i32, i32, P(vp)]),
+        "mlp_problem_info": (C.c_int, [vp, P(i32), P(i32), P(i32)]),
+        "mlp_problem_get_dist": (C.c_int, [vp, vp]),
+        "mlp_problem_destroy": (None, [vp]),
+        "mlp_solver_create": (C.c_int, [vp, i32, P(vp)]),
+        "mlp_solver_destroy": (None, [vp]),
+        "mlp_solver_set_stream": (C.c_int, [vp, vp]),
+        "mlp_solver_set_tile_shape": (C.c_int, [vp, i32]),
+        "mlp_solver_set_unroll": (C.c_int, [vp, i32]),
+        "mlp_solver_set_tour": (C.c_int, [vp, vp, i32]),
+        "mlp_solver_set_tour_device": (C.c_int, [vp, vp, i32]),
+        "mlp_solver_get_tour": (C.c_int, [vp, vp, i32]),
+        "mlp_solver_tour_device": (C.c_int, [vp, P(vp)]),
+        "mlp_solver_cost": (C.c_int, [vp, P(i64)]),
+        "mlp_solver_weights": (C.c_int, [vp, vp, i32]),
+        "mlp_solver_ads": (C.c_int, [vp, vp, i64]),
+        "mlp_solver_num_candidates": (C.c_int, [vp, i32, P(i32)]),
+        "mlp_solver_eval": (C.c_int, [vp, i32, vp, vp, vp]),
+        "mlp_solver_pass": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, P(i32), P(i64)]),
+        "mlp_solver_dvnd": (C.c_int, [vp, i32, i32, P(DvndStats)]),
+        "mlp_solver_begin": (C.c_int, [vp, i32, i32]),
+        "mlp_solver_enqueue": (C.c_int, [vp, i32]),
+        "mlp_solver_stats": (C.c_int, [vp, P(DvndStats)]),
+        "mlp_solver_sweep": (C.c_int, [vp, i32, i32, P(i64)]),
+        "mlp_solver_autotune": (C.c_int, [vp, P(i32)]),
+        "mlp_batch_create": (C.c_int, [i32, P(vp)]),
+        "mlp_batch_destroy": (None, [vp]),
+        "mlp_batch_set_stream": (C.c_int, [vp, vp]),
+        "mlp_batch_set_tile_shape": (C.c_int, [vp, i32]),
+        "mlp_batch_add": (C.c_int, [vp, vp, vp, i32, P(i32)]),
+        "mlp_batch_run": (C.c_int, [vp, i32, i32]),
+        "mlp_batch_reset": (C.c_int, [vp]),
+        "mlp_batch_result": (C.c_int, [vp, i32, vp, i32, P(DvndStats)]),
+        "bestNeighborSimple": (C.c_uint, [C.c_char_p, vp, C.c_uint, C.c_int]),
+        "bestNeighbor": (C.c_uint, [C.c_char_p, vp, C.c_uint, C.c_int, C.c_bool, C.c_uint, vp, vp, vp,
+                                    vp, vp, C.c_bool, C.c_uint, vp]),
+        "applyMoves": (C.c_uint, [C.c_char_p, vp, C.c_uint, C.c_uint, vp, vp, vp, vp]),
+        "getNoConflictMoves": (C.c_int, [C.c_uint, vp, vp, vp, vp, vp, vp, C.c_bool, C.c_bool]),
+        "noConflict": (C.c_bool, [C.c_ushort, C.c_uint, C.c_uint, C.c_ushort, C.c_uint, C.c_uint]),
+        "segFault": (None, []),
+        "mlp_legacy_reset": (None, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        raise MLPError(status, lib().mlp_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+
+
+def device_count() -> int:
+    c = C.c_int32(0)
+    st = lib().mlp_device_count(C.byref(c))
+    return c.value if st == 0 else 0
+
+
+class Problem:
+    """MLProblem: an instance resident on the GPU (n x n int32 distances)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        n, size, dmax = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(lib().mlp_problem_info(self._h, C.byref(n), C.byref(size), C.byref(dmax)))
+        self.n, self.size, self.max_dist = n.value, size.value, dmax.value
+
+    @classmethod
+    def from_coords(cls, x: Sequence[int], y: Sequence[int], dist_round: bool = True,
+                    cost_tour: bool = True) -> "Problem":
+        x, y = _i32(x), _i32(y)
+        h = C.c_void_p()
+        _check(lib().mlp_problem_create_coords(len(x), _ptr(x), _ptr(y), int(cost_tour),
+                                               int(dist_round), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_coords_device(cls, n: int, x_dev: int, y_dev: int, dist_round: bool = True) -> "Problem":
+        h = C.c_void_p()
+        _check(lib().mlp_problem_create_coords_device(n, C.c_void_p(x_dev), C.c_void_p(y_dev), 1,
+                                                      int(dist_round), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_matrix(cls, D: np.ndarray, cost_tour: bool = True) -> "Problem":
+        D = _i32(D)
+        h = C.c_void_p()
+        _check(lib().mlp_problem_create_matrix(D.shape[0], _ptr(D), int(cost_tour), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load_tsplib(cls, path: str, dist_round: bool = False, cost_tour: bool = True) -> "Problem":
+        h = C.c_void_p()
+        _check(lib().mlp_problem_load_tsplib(path.encode(), int(cost_tour), int(dist_round), C.byref(h)))
+        return cls(h)
+
+    def dist(self) -> np.ndarray:
+        D = np.zeros((self.n, self.n), np.int32)
+        _check(lib().mlp_problem_get_dist(self._h, _ptr(D)))
+        return D
+
+    def close(self) -> None:
+        if self._h:
+            lib().mlp_problem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """MLSolution + the MLKernel tasks of one instance (device-resident state)."""
+
+    def __init__(self, problem: Problem, wide: bool = False):
+        self.problem = problem
+        self.wide = bool(wide)
+        self._h = C.c_void_p()
+        _check(lib().mlp_solver_create(problem._h, int(wide), C.byref(self._h)))
+        self.size = problem.size
+
+    def close(self) -> None:
+        if self._h:
+            lib().mlp_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int) -> None:
+        _check(lib().mlp_solver_set_stream(self._h, C.c_void_p(stream_handle)))
+
+    def set_tile_shape(self, shape: int) -> None:
+        _check(lib().mlp_solver_set_tile_shape(self._h, shape))
+
+    def set_unroll(self, u: int) -> None:
+        _check(lib().mlp_solver_set_unroll(self._h, u))
+
+    def set_tour(self, tour: Sequence[int]) -> None:
+        t = _i32(tour)
+        _check(lib().mlp_solver_set_tour(self._h, _ptr(t), len(t)))
+
+    def set_tour_device(self, ptr: int) -> None:
+        _check(lib().mlp_solver_set_tour_device(self._h, C.c_void_p(ptr), self.size))
+
+    def tour(self) -> np.ndarray:
+        t = np.zeros(self.size, np.int32)
+        _check(lib().mlp_solver_get_tour(self._h, _ptr(t), self.size))
+        return t
+
+    def tour_device_ptr(self) -> int:
+        p = C.c_void_p()
+        _check(lib().mlp_solver_tour_device(self._h, C.byref(p)))
+        return p.value
+
+    def cost(self) -> int:
+        c = C.c_int64()
+        _check(lib().mlp_solver_cost(self._h, C.byref(c)))
+        return c.value
+
+    def weights(self) -> np.ndarray:
+        w = np.zeros(self.size, np.int32)
+        _check(lib().mlp_solver_weights(self._h, _ptr(w), self.size))
+        return w
+
+    def ads(self) -> np.ndarray:
+        words = 32 + self.size * (self.size + 3)
+        a = np.zeros(words, np.uint32)
+        _check(lib().mlp_solver_ads(self._h, _ptr(a), words))
+        return a
+
+    def num_candidates(self, nb: int) -> int:
+        c = C.c_int32()
+        _check(lib().mlp_solver_num_candidates(self._h, nb, C.byref(c)))
+        return c.value
+
+    def eval(self, nb: int):
+        m = self.num_candidates(nb)
+        cost = np.zeros(m, np.int64)
+        i = np.zeros(m, np.int32)
+        j = np.zeros(m, np.int32)
+        _check(lib().mlp_solver_eval(self._h, nb, _ptr(cost), _ptr(i), _ptr(j)))
+        return cost, i, j
+
+    def pass_(self, nb: int, max_moves: int = 1 << 15):
+        ids = np.zeros(max_moves, np.int32)
+        i = np.zeros(max_moves, np.int32)
+        j = np.zeros(max_moves, np.int32)
+        c = np.zeros(max_moves, np.int64)
+        cnt, nc = C.c_int32(), C.c_int64()
+        _check(lib().mlp_solver_pass(self._h, nb, max_moves, _ptr(ids), _ptr(i), _ptr(j), _ptr(c),
+                                     C.byref(cnt), C.byref(nc)))
+        k = min(cnt.value, max_moves)
+        return nc.value, list(zip(ids[:k].tolist(), i[:k].tolist(), j[:k].tolist(), c[:k].tolist()))
+
+    def dvnd(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> dict:
+        st = DvndStats()
+        _check(lib().mlp_solver_dvnd(self._h, nb_mask, max_iters, C.byref(st)))
+        return st.as_dict()
+
+    def begin(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> None:
+        _check(lib().mlp_solver_begin(self._h, nb_mask, max_iters))
+
+    def enqueue(self, iterations: int) -> None:
+        _check(lib().mlp_solver_enqueue(self._h, iterations))
+
+    def stats(self) -> dict:
+        st = DvndStats()
+        _check(lib().mlp_solver_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def sweep(self, nb_mask: int = NB_ALL, repeats: int = 1) -> int:
+        e = C.c_int64()
+        _check(lib().mlp_solver_sweep(self._h, nb_mask, repeats, C.byref(e)))
+        return e.value
+
+    def autotune(self) -> int:
+        s = C.c_int32()
+        _check(lib().mlp_solver_autotune(self._h, C.byref(s)))
+        return s.value
+
+
+class Batch:
+    """Batched form: many DVND searches advanced by the same launches."""
+
+    def __init__(self, wide: bool = False):
+        self._h = C.c_void_p()
+        _check(lib().mlp_batch_create(int(wide), C.byref(self._h)))
+        self.sizes: list[int] = []
+        self._problems: list[Problem] = []
+
+    def close(self) -> None:
+        if self._h:
+            lib().mlp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int) -> None:
+        _check(lib().mlp_batch_set_stream(self._h, C.c_void_p(stream_handle)))
+
+    def set_tile_shape(self, shape: int) -> None:
+        _check(lib().mlp_batch_set_tile_shape(self._h, shape))
+
+    def add(self, problem: Problem, tour: Sequence[int]) -> int:
+        t = _i32(tour)
+        j = C.c_int32()
+        _check(lib().mlp_batch_add(self._h, problem._h, _ptr(t), len(t), C.byref(j)))
+        self.sizes.append(len(t))
+        self._problems.append(problem)
+        return j.value
+
+    def run(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> None:
+        _check(lib().mlp_batch_run(self._h, nb_mask, max_iters))
+
+    def reset(self) -> None:
+        _check(lib().mlp_batch_reset(self._h))
+
+    def result(self, job: int):
+        t = np.zeros(self.sizes[job], np.int32)
+        st = DvndStats()
+        _check(lib().mlp_batch_result(self._h, job, _ptr(t), len(t), C.byref(st)))
+        return t, st.as_dict()
+
+
+class Legacy:
+    """The reference's extern "C" DVND entry points (include/wamca_dvnd.h)."""
+
+    @staticmethod
+    def best_neighbor(file: str, solution: np.ndarray, nb: int, just_calc: bool = False,
+                      host_code: int = 0, use_moves: int = 0, solution_resp: Optional[np.ndarray] = None):
+        sol = solution
+        um = C.c_uint(use_moves)
+        cap = max(use_moves, 1)
+        ids = np.zeros(cap, np.uint16)
+        is_ = np.zeros(cap, np.uint32)
+        js = np.zeros(cap, np.uint32)
+        cs = np.zeros(cap, np.int32)
+        resp_ptr = _ptr(solution_resp) if solution_resp is not None else None
+        r = lib().bestNeighbor(file.encode(), _ptr(sol), len(sol), nb, just_calc, host_code, C.byref(um),
+                               _ptr(ids), _ptr(is_), _ptr(js), _ptr(cs), False, 1, resp_ptr)
+        k = um.value if use_moves else 0
+        return r, list(zip(ids[:k].tolist(), is_[:k].tolist(), js[:k].tolist(), cs[:k].tolist()))
+
+    @staticmethod
+    def apply_moves(file: str, solution: np.ndarray, moves) -> int:
+        m = len(moves)
+        ids = np.array([mv[0] for mv in moves], np.uint16)
+        is_ = np.array([mv[1] for mv in moves], np.uint32)
+        js = np.array([mv[2] for mv in moves], np.uint32)
+        cs = np.array([mv[3] if len(mv) > 3 else 0 for mv in moves], np.int32)
+        return lib().applyMoves(file.encode(), _ptr(solution), len(solution), m, _ptr(ids), _ptr(is_),
+                                _ptr(js), _ptr(cs))
+
+    @staticmethod
+    def no_conflict_moves(moves, maximize: bool = False, melhor_para_pior: bool = False):
+        m = len(moves)
+        ids = np.array([mv[0] for mv in moves], np.uint16)
+        is_ = np.array([mv[1] for mv in moves], np.uint32)
+        js = np.array([mv[2] for mv in moves], np.uint32)
+        cs = np.array([mv[3] for mv in moves], np.int32)
+        sel = np.zeros(max(m, 1), np.int32)
+        imp = np.zeros(1, np.int32)
+        k = lib().getNoConflictMoves(m, _ptr(ids), _ptr(is_), _ptr(js), _ptr(cs), _ptr(sel), _ptr(imp),
+                                     maximize, melhor_para_pior)
+        return sel[:max(k, 0)].tolist(), int(imp[0]), k
+
+    @staticmethod
+    def no_conflict(id1, i1, j1, id2, i2, j2) -> bool:
+        return bool(lib().noConflict(id1, i1, j1, id2, i2, j2))
+
+    @staticmethod
+    def reset() -> None:
+        lib().mlp_legacy_reset()

@@ -106,7 +106,10 @@ MLP_API int mlp_solver_create(mlp_problem_t p, int32_t wide, mlp_solver_t* out);
 MLP_API void mlp_solver_destroy(mlp_solver_t s);
 /* Stream on which every later call of this solver runs (NULL: the solver's own). */
 MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
-/* Sweep tile shape index (0..5) and DVND iterations per CUDA-graph replay. */
+/* Sweep tile shape index (0..5).  Loop mode: iterations = 0 (default) runs the
+ * DVND loop on the device (a CUDA-graph while node, no host round trips);
+ * iterations >= 1 replays graphs of that many iterations and checks convergence
+ * on the host in between. */
 MLP_API int mlp_solver_set_tile_shape(mlp_solver_t s, int32_t shape);
 MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t iterations);
 /* Tour of `len` = size entries: tour[0] = tour[size-1] = 0 and a permutation of
@@ -140,13 +143,17 @@ MLP_API int mlp_solver_pass(mlp_solver_t s, int32_t nb, int32_t max_moves, int32
  * (at most max_iters sweeps).  Synchronous. */
 MLP_API int mlp_solver_dvnd(mlp_solver_t s, int32_t nb_mask, int32_t max_iters,
                             mlp_dvnd_stats_t* stats);
+/* Enqueue a whole DVND (device-side loop) on the solver's stream and return
+ * without waiting; read the result with mlp_solver_stats / get_tour. */
+MLP_API int mlp_solver_dvnd_async(mlp_solver_t s, int32_t nb_mask, int32_t max_iters);
 /* Enqueue `iterations` DVND iterations on the solver's stream without waiting
  * (call mlp_solver_begin first; read results with mlp_solver_stats). */
 MLP_API int mlp_solver_begin(mlp_solver_t s, int32_t nb_mask, int32_t max_iters);
 MLP_API int mlp_solver_enqueue(mlp_solver_t s, int32_t iterations);
 MLP_API int mlp_solver_stats(mlp_solver_t s, mlp_dvnd_stats_t* stats);
 /* Enqueue `repeats` evaluation-only sweeps of nb_mask (timing helper; the tour
- * is not changed).  *evals_per_sweep = move evaluations of one sweep. */
+ * is not changed): one tiny counter-reset kernel, `repeats` sweep kernels and
+ * one ADS rebuild.  *evals_per_sweep = move evaluations of one sweep. */
 MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats,
                              int64_t* evals_per_sweep);
 /* Autotune the sweep tile shape on the current tour; returns the chosen index. */
@@ -162,6 +169,8 @@ MLP_API int mlp_batch_add(mlp_batch_t b, mlp_problem_t p, const int32_t* tour, i
                           int32_t* job);
 /* Runs every job's DVND to a local optimum (at most max_iters sweeps each). */
 MLP_API int mlp_batch_run(mlp_batch_t b, int32_t nb_mask, int32_t max_iters);
+/* Same, enqueued on the batch's stream without waiting (device-side loop). */
+MLP_API int mlp_batch_run_async(mlp_batch_t b, int32_t nb_mask, int32_t max_iters);
 /* Resets every job to the tour it was added with (for repeated runs). */
 MLP_API int mlp_batch_reset(mlp_batch_t b);
 MLP_API int mlp_batch_result(mlp_batch_t b, int32_t job, int32_t* tour, int32_t len,

@@ -262,24 +262,10 @@ def legacy_apply_moves(tour, D, moves):
 
 
 # ---------------------------------------------------------------- generators
-def uniform_instance(n: int, seed: int, box: int = 1000):
-    """n points with integer coordinates uniform in [0, box]^2 (seeded)."""
-    r = np.random.default_rng(seed)
-    return r.integers(0, box + 1, n).astype(np.int32), r.integers(0, box + 1, n).astype(np.int32)
+# The benchmark's seeded generators live in the product package (pure numpy,
+# no GPU); they are re-exported here so tests can build the same inputs.
+import sys as _sys  # noqa: E402
 
-
-def clustered_instance(n: int, seed: int, clusters: int = 8, sigma: float = 50.0, box: int = 1000):
-    """n points from `clusters` Gaussian clusters (sigma) with centres uniform in
-    [0, box]^2, rounded and clipped to the box (seeded)."""
-    r = np.random.default_rng(seed)
-    centres = r.uniform(0, box, size=(clusters, 2))
-    lab = r.integers(0, clusters, n)
-    pts = centres[lab] + r.normal(0.0, sigma, size=(n, 2))
-    pts = np.clip(np.rint(pts), 0, box).astype(np.int32)
-    return pts[:, 0].copy(), pts[:, 1].copy()
-
-
-def random_perm_tour(n: int, seed: int) -> np.ndarray:
-    """Depot 0, a seeded random permutation of 1..n-1, depot 0."""
-    r = np.random.default_rng(seed + 1_000_003)
-    return np.concatenate([[0], 1 + r.permutation(n - 1), [0]]).astype(np.int32)
+_sys.path.insert(0, os.path.join(os.path.dirname(HERE), "wamca-gpu-mi_gb300"))
+from mlpgpu.workloads import (clustered_instance, log_uniform_sizes, random_perm_tour,  # noqa: E402,F401
+                              uniform_instance)

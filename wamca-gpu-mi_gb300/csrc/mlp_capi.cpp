@@ -213,6 +213,11 @@ MLP_API int mlp_solver_set_tile_shape(mlp_solver_t s, int32_t shape) {
 
 MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t u) {
   if (!s) return arg_error("null solver");
+  if (u == 0) {
+    s->set->set_device_loop(true);
+    return kOk;
+  }
+  s->set->set_device_loop(false);
   return s->set->set_unroll(u);
 }
 
@@ -374,6 +379,12 @@ MLP_API int mlp_solver_dvnd(mlp_solver_t s, int32_t nb_mask, int32_t max_iters, 
   return solver_stats(s, stats, nb_mask);
 }
 
+MLP_API int mlp_solver_dvnd_async(mlp_solver_t s, int32_t nb_mask, int32_t max_iters) {
+  if (!s) return arg_error("null solver");
+  MLP_TRY(s->set->set_mask(nb_mask));
+  return s->set->enqueue_device_loop(max_iters);
+}
+
 MLP_API int mlp_solver_begin(mlp_solver_t s, int32_t nb_mask, int32_t max_iters) {
   if (!s) return arg_error("null solver");
   if (max_iters <= 0) return arg_error("max_iters must be positive");
@@ -397,7 +408,8 @@ MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats, i
   if (!s) return arg_error("null solver");
   if (repeats < 0) return arg_error("repeats must be >= 0");
   MLP_TRY(s->set->set_mask(nb_mask));
-  for (int r = 0; r < repeats; r++) MLP_TRY(s->set->sweep_only());
+  MLP_CUDA(launch_stats_begin(s->set->device_jobs(), 1, 1, s->set->stream()), "stats kernel");
+  for (int r = 0; r < repeats; r++) MLP_TRY(s->set->sweep_kernel());
   MLP_TRY(s->set->prepare(false));
   if (evals_per_sweep) *evals_per_sweep = s->set->evals_per_sweep(0, nb_mask);
   return kOk;
@@ -523,6 +535,14 @@ MLP_API int mlp_batch_run(mlp_batch_t b, int32_t nb_mask, int32_t max_iters) {
   MLP_TRY(b->set->set_mask(nb_mask));
   b->mask = nb_mask;
   return b->set->run(max_iters, true);
+}
+
+MLP_API int mlp_batch_run_async(mlp_batch_t b, int32_t nb_mask, int32_t max_iters) {
+  if (!b) return arg_error("null batch");
+  MLP_TRY(batch_build(b));
+  MLP_TRY(b->set->set_mask(nb_mask));
+  b->mask = nb_mask;
+  return b->set->enqueue_device_loop(max_iters);
 }
 
 MLP_API int mlp_batch_result(mlp_batch_t b, int32_t job, int32_t* tour, int32_t len, mlp_dvnd_stats_t* stats) {

@@ -275,6 +275,7 @@ JobSet::JobSet(std::vector<Job*> jobs, bool wide, cudaStream_t stream)
 
 JobSet::~JobSet() {
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
   if (djobs_) cudaFree(djobs_);
   if (dtiles_) cudaFree(dtiles_);
   if (hstats_) cudaFreeHost(hstats_);
@@ -327,6 +328,8 @@ int JobSet::build_tiles() {
   }
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
+  if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
+  loop_graph_ = nullptr;
   if (dtiles_) cudaFree(dtiles_);
   dtiles_ = nullptr;
   ntiles_ = (int)tiles.size();
@@ -340,6 +343,8 @@ int JobSet::set_stream(cudaStream_t s) {
   stream_ = s;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
+  if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
+  loop_graph_ = nullptr;
   return kOk;
 }
 
@@ -395,6 +400,11 @@ int JobSet::sweep_only() {
   return kOk;
 }
 
+int JobSet::sweep_kernel() {
+  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
+  return kOk;
+}
+
 int JobSet::graph_for(int iters, cudaGraphExec_t* out) {
   auto it = graphs_.find(iters);
   if (it != graphs_.end()) {
@@ -439,10 +449,79 @@ int JobSet::enqueue_iterations(int iters) {
   return kOk;
 }
 
+int JobSet::enqueue_device_loop(int max_iters) {
+  if (max_iters <= 0) {
+    set_error("max_iters must be positive");
+    return kErrArg;
+  }
+  if (stream_ == 0) {
+    set_error("the device-side loop needs a non-default stream");
+    return kErrState;
+  }
+  const int unroll = 2;
+  if (!loop_graph_ || loop_unroll_ != unroll) {
+    if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
+    loop_graph_ = nullptr;
+    cudaGraph_t g;
+    MLP_CUDA(cudaGraphCreate(&g, 0), "graph create");
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return cuda_status(e, "conditional handle");
+    }
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return cuda_status(e, "conditional node");
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return cuda_status(e, "capture body");
+    }
+    int st = kOk;
+    for (int q = 0; q < unroll && st == kOk; q++) st = launch_iteration();
+    if (st == kOk) st = cuda_status(launch_loop_condition(djobs_, (int)jobs_.size(), h, stream_), "condition kernel");
+    cudaGraph_t captured;
+    cudaError_t e2 = cudaStreamEndCapture(stream_, &captured);
+    if (st != kOk) {
+      cudaGraphDestroy(g);
+      return st;
+    }
+    if (e2 != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return cuda_status(e2, "end capture");
+    }
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    MLP_CUDA(e, "graph instantiate");
+    loop_graph_ = ge;
+    loop_unroll_ = unroll;
+  }
+  MLP_CUDA(launch_stats_begin(djobs_, (int)jobs_.size(), max_iters, stream_), "stats kernel");
+  MLP_CUDA(cudaGraphLaunch(loop_graph_, stream_), "graph launch");
+  return kOk;
+}
+
 int JobSet::run(int max_iters, bool sync) {
   if (max_iters <= 0) {
     set_error("max_iters must be positive");
     return kErrArg;
+  }
+  if (device_loop_ && stream_ != 0) {
+    int st = enqueue_device_loop(max_iters);
+    if (st != kOk || !sync) return st;
+    std::vector<std::array<int64_t, kStatWords>> s;
+    return read_stats(&s);
   }
   MLP_CUDA(launch_stats_begin(djobs_, (int)jobs_.size(), max_iters, stream_), "stats kernel");
   int done = 0;

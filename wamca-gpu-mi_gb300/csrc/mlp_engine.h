@@ -99,16 +99,25 @@ class JobSet {
   int set_shape(int shape);
   int shape() const { return shape_; }
   int set_unroll(int u);
+  // true: DVND loops on the device (graph while-node); false: the host checks
+  // convergence after every `unroll` graph-replayed iterations.
+  void set_device_loop(bool on) { device_loop_ = on; }
   // Rebuild the ADS arrays and reset statistics (after new tours).
   int prepare(bool reset_stats);
   // Set the neighbourhood mask of every job (bit nb = neighbourhood nb).
   int set_mask(int mask);
   // One sweep only (keys left on the device; call prepare() afterwards).
   int sweep_only();
+  // The sweep kernel alone (after a sweep_only() or stats reset).
+  int sweep_kernel();
   // DVND iterations until every job converged or max_iters sweeps ran.
   int run(int max_iters, bool sync);
   // Enqueue `iters` iterations without host synchronisation (graph replay).
   int enqueue_iterations(int iters);
+  // Enqueue a whole DVND (at most max_iters sweeps per job) as one CUDA graph
+  // whose while-node loops on the device until every job converged; no host
+  // synchronisation.  Read the results with read_stats().
+  int enqueue_device_loop(int max_iters);
   int read_stats(std::vector<std::array<int64_t, kStatWords>>* out);
   int64_t evals_per_sweep(int job, int mask) const;
   const std::vector<Job*>& jobs() const { return jobs_; }
@@ -124,6 +133,7 @@ class JobSet {
   cudaStream_t stream_;
   int shape_ = -1;
   int unroll_ = 16;
+  bool device_loop_ = true;
   int mask_ = 0x1f;
   int max_size_ = 0;
   bool merge_smem_ = true;
@@ -133,6 +143,8 @@ class JobSet {
   int64_t* hstats_ = nullptr;  // pinned, kStatWords per job
   int64_t* dstats_ = nullptr;  // device, kStatWords per job (jobs' stats live here)
   std::map<int, cudaGraphExec_t> graphs_;
+  cudaGraphExec_t loop_graph_ = nullptr;
+  int loop_unroll_ = 0;
 };
 
 int default_shape(int size);

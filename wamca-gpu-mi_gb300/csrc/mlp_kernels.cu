@@ -786,6 +786,20 @@ __global__ void k_stats_begin(const JobDev* __restrict__ jobs, int njobs, int64_
   st[kStatLimit] = limit;
 }
 
+__global__ void k_loop_condition(const JobDev* __restrict__ jobs, int njobs, cudaGraphConditionalHandle h) {
+  __shared__ int s_any;
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  int any = 0;
+  for (int q = threadIdx.x; q < njobs; q += blockDim.x) {
+    const int64_t* st = jobs[q].stats;
+    if (!st[kStatConverged] && st[kStatSweeps] < st[kStatLimit]) any = 1;
+  }
+  if (any) s_any = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) cudaGraphSetConditional(h, s_any ? 1u : 0u);
+}
+
 template <bool WIDE, int TL, int TR>
 cudaError_t sweep_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, cudaStream_t s) {
   k_sweep<WIDE, TL, TR><<<ntiles, TL, 0, s>>>(tiles, jobs);
@@ -839,6 +853,12 @@ cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem
   const size_t smem = use_smem ? MergeLayout(max_size).total : 0;
   if (wide) k_merge<true><<<njobs * kNumNb, 1024, smem, s>>>(jobs, use_smem ? 1 : 0);
   else k_merge<false><<<njobs * kNumNb, 1024, smem, s>>>(jobs, use_smem ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_loop_condition(const JobDev* jobs, int njobs, cudaGraphConditionalHandle h,
+                                  cudaStream_t s) {
+  k_loop_condition<<<1, 256, 0, s>>>(jobs, njobs, h);
   return cudaGetLastError();
 }
 

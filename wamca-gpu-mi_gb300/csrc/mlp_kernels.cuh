@@ -27,6 +27,10 @@ int merge_smem_max_size();
 // Opt the merge kernels into `bytes` of dynamic shared memory (call before
 // launching or capturing merges that use shared memory).
 cudaError_t configure_merge(size_t bytes);
+// Sets the CUDA-graph while-condition: 1 while some job is neither converged
+// nor at its sweep limit (the device-side DVND loop).
+cudaError_t launch_loop_condition(const JobDev* jobs, int njobs, cudaGraphConditionalHandle h,
+                                  cudaStream_t s);
 // Zero the run counters of every job and set its sweep limit.
 cudaError_t launch_stats_begin(const JobDev* jobs, int njobs, int64_t limit, cudaStream_t s);
 cudaError_t launch_prepare(const JobDev* jobs, int njobs, bool wide, bool reset_stats,

@@ -92,6 +92,8 @@ def lib() -> C.CDLL:
         "mlp_solver_pass": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, P(i32), P(i64)]),
         "mlp_solver_dvnd": (C.c_int, [vp, i32, i32, P(DvndStats)]),
         "mlp_solver_begin": (C.c_int, [vp, i32, i32]),
+        "mlp_solver_dvnd_async": (C.c_int, [vp, i32, i32]),
+        "mlp_batch_run_async": (C.c_int, [vp, i32, i32]),
         "mlp_solver_enqueue": (C.c_int, [vp, i32]),
         "mlp_solver_stats": (C.c_int, [vp, P(DvndStats)]),
         "mlp_solver_sweep": (C.c_int, [vp, i32, i32, P(i64)]),
@@ -287,6 +289,9 @@ class Solver:
         _check(lib().mlp_solver_dvnd(self._h, nb_mask, max_iters, C.byref(st)))
         return st.as_dict()
 
+    def dvnd_async(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> None:
+        _check(lib().mlp_solver_dvnd_async(self._h, nb_mask, max_iters))
+
     def begin(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> None:
         _check(lib().mlp_solver_begin(self._h, nb_mask, max_iters))
 
@@ -345,6 +350,9 @@ class Batch:
 
     def run(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> None:
         _check(lib().mlp_batch_run(self._h, nb_mask, max_iters))
+
+    def run_async(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> None:
+        _check(lib().mlp_batch_run_async(self._h, nb_mask, max_iters))
 
     def reset(self) -> None:
         _check(lib().mlp_batch_reset(self._h))

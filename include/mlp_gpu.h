@@ -106,7 +106,8 @@ MLP_API int mlp_solver_create(mlp_problem_t p, int32_t wide, mlp_solver_t* out);
 MLP_API void mlp_solver_destroy(mlp_solver_t s);
 /* Stream on which every later call of this solver runs (NULL: the solver's own). */
 MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
-/* Sweep tile shape index (0..5).  Loop mode: iterations = 0 (default) runs the
+/* Sweep tile shape index (0..7: diagonals x rows = 32x4, 32x8, 32x16, 64x4, 64x8,
+ * 64x16, 128x8, 128x16).  Loop mode: iterations = 0 (default) runs the
  * DVND loop on the device (a CUDA-graph while node, no host round trips);
  * iterations >= 1 replays graphs of that many iterations and checks convergence
  * on the host in between. */

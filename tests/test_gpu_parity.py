@@ -47,7 +47,7 @@ def test_candidates_all_neighbourhoods(mlpgpu_mod, n, seed, wide):
         assert np.array_equal(i, oi) and np.array_equal(j, oj), f"nb {nb}: moves differ"
 
 
-@pytest.mark.parametrize("shape", range(6))
+@pytest.mark.parametrize("shape", range(8))
 def test_candidates_every_tile_shape(mlpgpu_mod, shape):
     n = 333
     x, y = oracle.clustered_instance(n, 11)
@@ -200,3 +200,28 @@ def test_matrix_problem_and_errors(mlpgpu_mod):
     # the solver still works after rejected calls
     s.set_tour(t)
     assert s.dvnd()["cost"] == oracle.dvnd(t, D)[1]["cost"]
+
+
+def test_large_sizes_use_global_merge_workspace(mlpgpu_mod):
+    """Sizes beyond the shared-memory merge run the merge from a global
+    workspace; alone and mixed with small jobs in one batch."""
+    n = 1900
+    x, y = oracle.uniform_instance(n, 51)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, 51)
+    p = mlpgpu_mod.Problem.from_coords(x, y, dist_round=True)
+    s = mlpgpu_mod.Solver(p)
+    s.set_tour(t)
+    st = s.dvnd(max_iters=6)
+    ot, ost = oracle.dvnd(t, D, max_iters=6, threads=8)
+    assert np.array_equal(s.tour(), ot) and st["cost"] == ost["cost"]
+    b = mlpgpu_mod.Batch()
+    xs, ys = oracle.uniform_instance(80, 52)
+    Ds = oracle.dist(xs, ys, True)
+    ts = oracle.random_perm_tour(80, 52)
+    ps = mlpgpu_mod.Problem.from_coords(xs, ys, dist_round=True)
+    b.add(ps, ts)
+    b.add(p, t)
+    b.run(max_iters=6)
+    assert np.array_equal(b.result(0)[0], oracle.dvnd(ts, Ds, max_iters=6)[0])
+    assert np.array_equal(b.result(1)[0], ot)

@@ -343,7 +343,10 @@ MLP_API int mlp_solver_pass(mlp_solver_t s, int32_t nb, int32_t max_moves, int32
   if (nb < 0 || nb >= kNumNb) return arg_error("neighbourhood out of range");
   if (max_moves > 0 && (!ids || !is || !js || !costs)) return arg_error("null move arrays");
   MLP_TRY(s->set->set_mask(1 << nb));
-  MLP_TRY(s->set->run(1, true));
+  MLP_TRY(s->set->set_record_moves(true));
+  const int rs = s->set->run(1, true);
+  MLP_TRY(s->set->set_record_moves(false));
+  MLP_TRY(rs);
   mlp_dvnd_stats_t st;
   std::vector<std::array<int64_t, kStatWords>> raw;
   MLP_TRY(s->set->read_stats(&raw));

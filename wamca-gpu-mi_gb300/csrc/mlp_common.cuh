@@ -165,6 +165,36 @@ MLP_HD void conflict_interval(int id, int i, int j, int& a, int& b) {
   }
 }
 
+// Branch-free form of !canMerge for the cross-neighbourhood merge.  A move's
+// shape is its type (0 swap, 1 2-opt, 2 Or-opt) and two closed core intervals:
+// swap {i}, {j}; 2-opt [i, j] twice; Or-opt-k [min, max+k] twice.  Two moves
+// conflict iff a core interval of the lower type meets a core interval of the
+// higher type widened by one position on the left (unless both are Or-opt)
+// and on the right (unless the higher type is Or-opt).  Exhaustively equal to
+// !canMerge (mlkernel.cu:649-729) over every move pair of small tours.
+MLP_HD uint64_t move_shape(int id, int i, int j) {
+  uint64_t t, a1, b1, a2, b2;
+  if (id == 0) {
+    t = 0; a1 = b1 = (uint64_t)i; a2 = b2 = (uint64_t)j;
+  } else if (id == 1) {
+    t = 1; a1 = a2 = (uint64_t)i; b1 = b2 = (uint64_t)j;
+  } else {
+    t = 2; a1 = a2 = (uint64_t)imin_(i, j); b1 = b2 = (uint64_t)(imax_(i, j) + id - 1);
+  }
+  return (t << 60) | (a1 << 45) | (b1 << 30) | (a2 << 15) | b2;
+}
+MLP_HD bool shapes_conflict(uint64_t s1, uint64_t s2) {
+  const int t1 = (int)(s1 >> 60), t2 = (int)(s2 >> 60);
+  const uint64_t lo = t1 <= t2 ? s1 : s2, hi = t1 <= t2 ? s2 : s1;
+  const int el = imin_(t1, t2) == 2 ? 0 : 1, er = imax_(t1, t2) == 2 ? 0 : 1;
+  const int la1 = (int)((lo >> 45) & 0x7fff), lb1 = (int)((lo >> 30) & 0x7fff);
+  const int la2 = (int)((lo >> 15) & 0x7fff), lb2 = (int)(lo & 0x7fff);
+  const int ha1 = (int)((hi >> 45) & 0x7fff) - el, hb1 = (int)((hi >> 30) & 0x7fff) + er;
+  const int ha2 = (int)((hi >> 15) & 0x7fff) - el, hb2 = (int)(hi & 0x7fff) + er;
+  return (la1 <= hb1 && ha1 <= lb1) | (la1 <= hb2 && ha2 <= lb1) | (la2 <= hb1 && ha1 <= lb2) |
+         (la2 <= hb2 && ha2 <= lb2);
+}
+
 // ---------------- device job descriptor ----------------
 // All pointers are device pointers.  Arrays of per-position data are padded
 // to size + 8 entries (zero beyond size - 1).
@@ -203,7 +233,7 @@ enum : int {
   kStatWords = 16
 };
 
-enum : int { kFlagWide = 1 };
+enum : int { kFlagWide = 1, kFlagRecordMoves = 2 };
 
 // Sweep work item: one parallelogram tile of the (row r, diagonal L) plane.
 struct SweepTile {

@@ -264,9 +264,9 @@ int job_create(Problem* p, bool wide, int moves_cap, Job** out) {
 }
 
 int default_shape(int size) {
-  if (size <= 320) return 0;    // 32 x 16
-  if (size <= 1400) return 2;   // 64 x 16
-  return 5;                     // 128 x 32
+  if (size <= 400) return 0;    // 32 diagonals x 4 rows
+  if (size <= 2000) return 1;   // 32 x 8
+  return 7;                     // 128 x 16
 }
 
 // ---------------------------------------------------------------- JobSet
@@ -280,6 +280,7 @@ JobSet::~JobSet() {
   if (dtiles_) cudaFree(dtiles_);
   if (hstats_) cudaFreeHost(hstats_);
   if (dstats_) cudaFree(dstats_);
+  for (void* p : extra_ws_) cudaFree(p);
 }
 
 int JobSet::init() {
@@ -297,13 +298,16 @@ int JobSet::init() {
   }
   merge_smem_ = max_size_ <= merge_smem_max_size();
   if (!merge_smem_) {
-    for (Job* j : jobs_)
-      if (j->dev.ws == nullptr) {
-        set_error("a job set mixing sizes above and below 2044 needs every job sized above it");
-        return kErrUnsupported;
-      }
+    // The merge runs from global workspaces: give one to every job lacking it.
+    for (Job* j : jobs_) {
+      if (j->dev.ws != nullptr) continue;
+      void* p = nullptr;
+      MLP_CUDA(cudaMalloc(&p, merge_ws_bytes(j->size)), "cudaMalloc(merge workspace)");
+      extra_ws_.push_back(p);
+      j->dev.ws = static_cast<uint8_t*>(p);
+    }
   }
-  if (merge_smem_) MLP_CUDA(configure_merge(merge_smem_bytes(max_size_)), "configure merge");
+  MLP_CUDA(configure_merge(merge_smem_ ? merge_smem_bytes(max_size_) : 0), "configure merge");
   MLP_CUDA(cudaMallocHost(&hstats_, sizeof(int64_t) * kStatWords * jobs_.size()), "cudaMallocHost");
   MLP_CUDA(cudaMalloc(&dstats_, sizeof(int64_t) * kStatWords * jobs_.size()), "cudaMalloc(stats)");
   MLP_CUDA(cudaMemset(dstats_, 0, sizeof(int64_t) * kStatWords * jobs_.size()), "memset(stats)");
@@ -380,6 +384,20 @@ int JobSet::set_mask(int mask) {
              "set mask");
   }
   MLP_CUDA(cudaStreamSynchronize(stream_), "set mask");
+  return kOk;
+}
+
+int JobSet::set_record_moves(bool on) {
+  for (size_t q = 0; q < jobs_.size(); q++) {
+    int32_t f = jobs_[q]->dev.flags;
+    f = on ? (f | kFlagRecordMoves) : (f & ~kFlagRecordMoves);
+    if (f == jobs_[q]->dev.flags) continue;
+    jobs_[q]->dev.flags = f;
+    MLP_CUDA(cudaMemcpyAsync(&djobs_[q].flags, &jobs_[q]->dev.flags, sizeof(int32_t), cudaMemcpyHostToDevice,
+                             stream_),
+             "set flags");
+  }
+  MLP_CUDA(cudaStreamSynchronize(stream_), "set flags");
   return kOk;
 }
 

@@ -106,6 +106,8 @@ class JobSet {
   int prepare(bool reset_stats);
   // Set the neighbourhood mask of every job (bit nb = neighbourhood nb).
   int set_mask(int mask);
+  // Record the applied moves of each iteration (for the legacy move vectors).
+  int set_record_moves(bool on);
   // One sweep only (keys left on the device; call prepare() afterwards).
   int sweep_only();
   // The sweep kernel alone (after a sweep_only() or stats reset).
@@ -142,6 +144,7 @@ class JobSet {
   int ntiles_ = 0;
   int64_t* hstats_ = nullptr;  // pinned, kStatWords per job
   int64_t* dstats_ = nullptr;  // device, kStatWords per job (jobs' stats live here)
+  std::vector<void*> extra_ws_;  // merge workspaces allocated for jobs of mixed-size sets
   std::map<int, cudaGraphExec_t> graphs_;
   cudaGraphExec_t loop_graph_ = nullptr;
   int loop_unroll_ = 0;

@@ -4,21 +4,27 @@
 //   k_sweep   all five neighbourhoods (swap, 2-opt, Or-opt-1/2/3) over the
 //             tour, tiled over (row r, diagonal L = c - r) parallelograms; one
 //             64-bit (delta, ctx) key per reference block via atomicMin.
-//   k_merge   one CTA per (job, neighbourhood): stage-2 greedy independent set
-//             (the reference's per-kernel GPU merge); the last CTA of a job runs
-//             the cross-neighbourhood greedy, applies the selected moves,
-//             rebuilds w / prefix arrays / cost and resets the candidate keys.
+//   k_merge   a cluster of six CTAs per job: five run the stage-2 greedy
+//             independent set of one neighbourhood each (the reference's
+//             per-kernel GPU merge) and pass the kept moves to the sixth over
+//             distributed shared memory; it runs the cross-neighbourhood
+//             greedy, applies the selected moves, rebuilds w / prefix arrays /
+//             cost and resets the candidate keys.
 //   k_prepare the ADS prefix rebuild alone (after a new tour is set).
 //
 // All arithmetic is integer.  In int32 mode every delta and cost is computed in
 // uint32 modular arithmetic, which reproduces the reference's 32-bit wrap-around
 // results exactly; in wide mode everything is int64.
+#include <cooperative_groups.h>
+
 #include <cstdint>
 
 #include "mlp_common.cuh"
 #include "mlp_kernels.cuh"
 
 namespace mlp {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -73,17 +79,66 @@ __device__ T block_exclusive_scan(T v, T* sm, T& total) {
   return before + x - v;
 }
 
+// Three block-wide scans at once (one set of barriers): exclusive prefixes of
+// a and b, totals of a, b and c.
+template <typename T>
+__device__ void block_exclusive_scan3(T a, T b, T c, T* sa, T* sb, T* sc, T& ea, T& eb, T& ta, T& tb,
+                                      T& tc) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  T xa = a, xb = b, xc = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T ya = __shfl_up_sync(kFull, xa, o), yb = __shfl_up_sync(kFull, xb, o),
+            yc = __shfl_up_sync(kFull, xc, o);
+    if (lane >= o) {
+      xa += ya;
+      xb += yb;
+      xc += yc;
+    }
+  }
+  if (lane == 31) {
+    sa[wid] = xa;
+    sb[wid] = xb;
+    sc[wid] = xc;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    T pa = lane < nw ? sa[lane] : T(0), pb = lane < nw ? sb[lane] : T(0), pc = lane < nw ? sc[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T ya = __shfl_up_sync(kFull, pa, o), yb = __shfl_up_sync(kFull, pb, o),
+              yc = __shfl_up_sync(kFull, pc, o);
+      if (lane >= o) {
+        pa += ya;
+        pb += yb;
+        pc += yc;
+      }
+    }
+    sa[lane] = pa;
+    sb[lane] = pb;
+    sc[lane] = pc;
+  }
+  __syncthreads();
+  ea = (wid > 0 ? sa[wid - 1] : T(0)) + xa - a;
+  eb = (wid > 0 ? sb[wid - 1] : T(0)) + xb - b;
+  ta = sa[nw - 1];
+  tb = sb[nw - 1];
+  tc = sc[nw - 1];
+  __syncthreads();
+}
+
 // --------------------------------------------------------------------------
 // ADS prefix rebuild: w[p] = D[t[p-1]][t[p]], W = prefix(w), Q = prefix(p w),
 // A[k-1][p] = D[t[p-1]][t[p+k]], cost = sum (size - p) w[p]
 // (source/mlsolution.cpp:216-228 and :454-458 for T = W).
 // --------------------------------------------------------------------------
 template <bool WIDE>
-__device__ void cta_prepare(const JobDev* J) {
+__device__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t* w_s) {
   using C = typename Arith<WIDE>::C;
   __shared__ C smW[32], smQ[32], smC[32];
   const int sz = J->size, n = J->n, pad = sz + 8;
-  const int32_t* __restrict__ t = J->tour;
+  const int32_t* __restrict__ t = t_override ? t_override : J->tour;
   const int32_t* __restrict__ D = J->D;
   int32_t* w = J->w;
   int32_t* A = J->A;
@@ -96,21 +151,20 @@ __device__ void cta_prepare(const JobDev* J) {
   C sW = 0, sQ = 0, sC = 0;
   for (int p = p0; p < p1; p++) {
     const int32_t prev = p > 0 ? t[p - 1] : 0;
-    const int32_t wp = p > 0 ? __ldg(D + (size_t)prev * n + t[p]) : 0;
+    const int32_t wp = p > 0 ? D[(size_t)prev * n + t[p]] : 0;
     w[p] = wp;
+    w_s[p] = wp;
     sW += (C)wp;
     sQ += (C)p * (C)wp;
     sC += (C)(sz - p) * (C)wp;
 #pragma unroll
     for (int k = 1; k <= 3; k++)
-      A[(k - 1) * pad + p] = (p >= 1 && p + k <= sz - 1) ? __ldg(D + (size_t)prev * n + t[p + k]) : 0;
+      A[(k - 1) * pad + p] = (p >= 1 && p + k <= sz - 1) ? D[(size_t)prev * n + t[p + k]] : 0;
   }
-  C totW, totQ, totC;
-  C eW = block_exclusive_scan<C>(sW, smW, totW);
-  C eQ = block_exclusive_scan<C>(sQ, smQ, totQ);
-  block_exclusive_scan<C>(sC, smC, totC);
+  C totW, totQ, totC, eW, eQ;
+  block_exclusive_scan3<C>(sW, sQ, sC, smW, smQ, smC, eW, eQ, totW, totQ, totC);
   for (int p = p0; p < p1; p++) {
-    const C wp = (C)w[p];
+    const C wp = (C)w_s[p];
     eW += wp;
     eQ += (C)p * wp;
     W[p] = eW;
@@ -133,12 +187,13 @@ __device__ void cta_reset_keys(const JobDev* J) {
 
 template <bool WIDE>
 __global__ void __launch_bounds__(1024) k_prepare(const JobDev* __restrict__ jobs, int reset_stats) {
+  extern __shared__ int32_t prep_w[];
   const JobDev* J = jobs + blockIdx.x;
   if (reset_stats && threadIdx.x < kStatWords) {
     const int q = threadIdx.x;
     if (q != kStatLimit) J->stats[q] = 0;
   }
-  cta_prepare<WIDE>(J);
+  cta_prepare<WIDE>(J, nullptr, prep_w);
   cta_reset_keys(J);
 }
 
@@ -221,12 +276,30 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
     for (int k = 0; k < 3; k++) sCA[k][q] = ok ? Ag[k * pad + p] : 0;
   }
   __syncthreads();
-  for (int idx = tid; idx < SR * SC; idx += TL) {
-    const int a = idx / SC, b = idx - a * SC;
-    const int rp = r0 - 1 + a, cp = rp + L0 - 1 + b;
-    int32_t v = 0;
-    if (rp <= sz - 1 && cp <= sz - 1) v = __ldg(D + (size_t)sRowT[a] * n + sColT[a + b]);
-    sS[a][b] = v;
+  {
+    // All gathers of the tile are issued before any is stored, so their
+    // latencies overlap (one L2/HBM round trip per tile instead of one per load).
+    constexpr int NG = (SR * SC + TL - 1) / TL;
+    int32_t gv[NG];
+#pragma unroll
+    for (int u = 0; u < NG; u++) {
+      const int idx = tid + u * TL;
+      int32_t v = 0;
+      if (idx < SR * SC) {
+        const int a = idx / SC, b = idx - a * SC;
+        const int rp = r0 - 1 + a, cp = rp + L0 - 1 + b;
+        if (rp <= sz - 1 && cp <= sz - 1) v = __ldg(D + (size_t)sRowT[a] * n + sColT[a + b]);
+      }
+      gv[u] = v;
+    }
+#pragma unroll
+    for (int u = 0; u < NG; u++) {
+      const int idx = tid + u * TL;
+      if (idx < SR * SC) {
+        const int a = idx / SC, b = idx - a * SC;
+        sS[a][b] = gv[u];
+      }
+    }
   }
   __syncthreads();
 
@@ -359,21 +432,59 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
 // --------------------------------------------------------------------------
 enum : uint8_t { kNone = 0, kUndec = 1, kIn = 2, kOut = 3 };
 
-// Workspace layout (bytes) of one merge CTA for a given size.
+// Stage-2 candidate record: one 128-bit shared-memory access per candidate.
+struct __align__(16) Rec {
+  uint64_t key;  // (delta, block) order key
+  uint32_t ab;   // swap: i | j << 16; 2-opt / Or-opt: conflict interval a | b << 16
+  uint32_t st;   // kNone / kUndec / kIn / kOut
+};
+constexpr int kBitMax = 512;         // stage-3 conflict bit-matrix capacity (moves)
+constexpr int kMergeThreads = 1024;
+constexpr int kClusterCtas = 6;  // five stage-2 CTAs and the stage-3 leader
+
+// Workspace layout (bytes) of the merge CTA of a job of a given size.
+//   A: per-candidate key / move / state of the five neighbourhoods (stage 2);
+//      reused for the apply owner map once stage 3 has compacted the kept set
+//   B: swap endpoint tables (stage 2), then the stage-3 move list and bit rows
+//   T: the old and the new tour
+__host__ __device__ __forceinline__ int region_cap(int nb, int size) {
+  const int div[kNumNb] = {4, 2, 3, 4, 5};
+  return size / div[nb] + 2;
+}
+__host__ __device__ __forceinline__ int region_off(int nb, int size) {
+  int o = 0;
+  for (int q = 0; q < nb; q++) o += region_cap(q, size);
+  return o;
+}
+
 struct MergeLayout {
-  int mmax, P, tb;
-  size_t cand, structs, stage2, stage3, total;
+  int tb, mmax, m3cap;
+  // stage-2 CTA: records, moves, swap tables
+  size_t o_ij2, o_tab, s2;
+  // leader: stage-3 list, conflict bits, owner map, old and new tour
+  size_t o_key3, o_shp3, o_ij3, o_st3, o_bits, o_owner, o_told, o_tnew, s3;
+  size_t total;
   __host__ __device__ explicit MergeLayout(int size) {
-    mmax = nb_blocks(2, size);
-    P = 1;
-    while (P < size + 4) P <<= 1;
     tb = total_blocks(size);
-    cand = align_up((size_t)mmax * 13, 16);
-    const size_t swapB = (size_t)2 * (size + 4) * 8, ivB = (size_t)8 * P * 8;
-    structs = swapB > ivB ? swapB : ivB;
-    stage2 = cand + structs;
-    stage3 = align_up((size_t)tb * 13, 16) + align_up((size_t)size * 4, 16);
-    total = align_up(stage2 > stage3 ? stage2 : stage3, 128);
+    mmax = nb_blocks(2, size);
+    // Kept moves of stage 2 are independent sets: at most size/4 + 1 swaps,
+    // size/3 + 1 2-opt and size/(k+2) + 1 Or-opt-k moves; each neighbourhood
+    // gets a region of the leader's list of at least that capacity.
+    m3cap = 0;
+    for (int nb = 0; nb < kNumNb; nb++) m3cap += region_cap(nb, size);
+    o_ij2 = align_up((size_t)mmax * sizeof(Rec), 16);
+    o_tab = o_ij2 + align_up((size_t)mmax * 4, 16);
+    s2 = o_tab + align_up((size_t)3 * (size + 4) * 8, 16);
+    o_key3 = 0;
+    o_shp3 = o_key3 + align_up((size_t)m3cap * 8, 16);
+    o_ij3 = o_shp3 + align_up((size_t)m3cap * 8, 16);
+    o_st3 = o_ij3 + align_up((size_t)m3cap * 4, 16);
+    o_bits = o_st3 + align_up((size_t)m3cap, 16);
+    o_owner = o_bits + (size_t)kBitMax * (kBitMax / 32) * 4;
+    o_told = o_owner + align_up((size_t)size * 4, 16);
+    o_tnew = o_told + align_up((size_t)size * 4, 16);
+    s3 = o_tnew + align_up((size_t)size * 4, 16);
+    total = align_up(s2 > s3 ? s2 : s3, 128);
   }
 };
 
@@ -381,199 +492,417 @@ __device__ __forceinline__ void amin(uint64_t* p, uint64_t v) {
   atomicMin((unsigned long long*)p, (unsigned long long)v);
 }
 
-// Stage 2: greedy independent set of one neighbourhood's negative candidates
-// in (delta, block) order with the same-neighbourhood predicate of the
-// reference's GPU merge (mlkernel.cu:51-170 after the sort at :256).  Computed
-// as the lexicographically-first maximal independent set by rounds; conflicts
-// are found with point tables (swap) or segment trees (interval moves).
-__device__ void stage2(const JobDev* J, int nb, uint8_t* ws, int* s_cnt) {
-  const int sz = J->size, tid = threadIdx.x, nt = blockDim.x;
-  const MergeLayout lay(sz);
-  const int m = nb_blocks(nb, sz), off = nb_offset(nb, sz);
-  uint64_t* skey = (uint64_t*)ws;
-  uint32_t* ij = (uint32_t*)(skey + lay.mmax);
-  uint8_t* st = (uint8_t*)(ij + lay.mmax);
-  uint64_t* sb = (uint64_t*)(ws + lay.cand);
-  const uint64_t* keys = J->keys;
-  if (tid == 0) *s_cnt = 0;
-  for (int x = tid; x < m; x += nt) {
-    const uint64_t key = keys[off + x];
-    uint8_t s = kNone;
-    if (key != kKeyNone) {
-      const int64_t cost = key_cost(key, kCtxBits);
-      if (cost < 0) {
-        int i, j;
-        map_move(nb, sz, x, (int)(key & ((1u << kCtxBits) - 1)), i, j);
-        skey[x] = make_key(cost, (uint32_t)x, kCtxBits);
-        ij[x] = (uint32_t)i | ((uint32_t)j << 16);
-        s = kUndec;
-      }
-    }
-    st[x] = s;
-  }
-  const int P = lay.P;
-  uint64_t* minB = sb;                 // swap: endpoint tables
-  uint64_t* minK = sb + (sz + 4);
-  uint64_t* covB = sb;                 // intervals: range-update / point-query trees
-  uint64_t* covK = sb + 2 * P;
-  uint64_t* stB = sb + 4 * P;          // point-update / range-query trees
-  uint64_t* stK = sb + 6 * P;
-  const int nclear = nb == 0 ? 2 * (sz + 4) : 8 * P;
-  for (int round = 0; round <= m; round++) {
-    for (int q = tid; q < nclear; q += nt) sb[q] = kKeyNone;
-    __syncthreads();
-    for (int x = tid; x < m; x += nt) {
-      const uint8_t s = st[x];
-      if (s != kUndec && s != kIn) continue;
-      const uint64_t v = skey[x];
-      const int i = (int)(ij[x] & 0xffff), j = (int)(ij[x] >> 16);
-      if (nb == 0) {
-        amin(&minB[i], v);
-        amin(&minB[j], v);
-        if (s == kIn) {
-          amin(&minK[i], v);
-          amin(&minK[j], v);
-        }
-      } else {
-        int a0, b0;
-        conflict_interval(nb, i, j, a0, b0);
-        for (int l = a0 + P, r = b0 + P + 1; l < r; l >>= 1, r >>= 1) {
-          if (l & 1) {
-            amin(&covB[l], v);
-            if (s == kIn) amin(&covK[l], v);
-            l++;
-          }
-          if (r & 1) {
-            --r;
-            amin(&covB[r], v);
-            if (s == kIn) amin(&covK[r], v);
-          }
-        }
-        for (int p = a0 + P; p >= 1; p >>= 1) {
-          amin(&stB[p], v);
-          if (s == kIn) amin(&stK[p], v);
-        }
-      }
-    }
-    __syncthreads();
-    int any = 0;
-    for (int x = tid; x < m; x += nt) {
-      if (st[x] != kUndec) continue;
-      const uint64_t v = skey[x];
-      const int i = (int)(ij[x] & 0xffff), j = (int)(ij[x] >> 16);
-      uint64_t qB = kKeyNone, qK = kKeyNone;
-      if (nb == 0) {
-#pragma unroll
-        for (int e = -1; e <= 1; e++) {
-          qB = min(qB, min(minB[i + e], minB[j + e]));
-          qK = min(qK, min(minK[i + e], minK[j + e]));
-        }
-      } else {
-        int a0, b0;
-        conflict_interval(nb, i, j, a0, b0);
-        for (int p = a0 + P; p >= 1; p >>= 1) {
-          qB = min(qB, covB[p]);
-          qK = min(qK, covK[p]);
-        }
-        for (int l = a0 + 1 + P, r = b0 + 1 + P; l < r; l >>= 1, r >>= 1) {
-          if (l & 1) {
-            qB = min(qB, stB[l]);
-            qK = min(qK, stK[l]);
-            l++;
-          }
-          if (r & 1) {
-            --r;
-            qB = min(qB, stB[r]);
-            qK = min(qK, stK[r]);
-          }
-        }
-      }
-      if (qK < v) st[x] = kOut;
-      else if (qB >= v) st[x] = kIn;
-      else any = 1;
-    }
-    if (!__syncthreads_or(any)) break;
-  }
-  uint64_t* kept = J->kept;
-  for (int x = tid; x < m; x += nt) {
-    if (st[x] != kIn) continue;
-    const int q = atomicAdd(s_cnt, 1);
-    const int64_t cost = key_cost(skey[x], kCtxBits);
-    kept[2 * (off + q)] = make_key(cost, ((uint32_t)nb << kCtxBits) | (uint32_t)x, kCtxBits + 3);
-    kept[2 * (off + q) + 1] = ij[x];
-  }
-  __syncthreads();
-  if (tid == 0) J->kept_count[nb] = *s_cnt;
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
+  const uint32_t hi = __reduce_min_sync(kFull, (uint32_t)(v >> 32));
+  const uint32_t lo = __reduce_min_sync(kFull, (uint32_t)(v >> 32) == hi ? (uint32_t)v : 0xffffffffu);
+  return ((uint64_t)hi << 32) | lo;
 }
 
-// Stage 3 (cross-neighbourhood greedy with canMerge, mlkernel.cu:649-864 with a
-// stable order), parallel apply of the selected moves (footprints are disjoint
-// for every pair canMerge accepts), prefix rebuild and key reset.
-template <bool WIDE>
-__device__ void stage3_apply(const JobDev* J, uint8_t* ws) {
-  __shared__ int s_m3, s_ns;
-  const int sz = J->size, tid = threadIdx.x, nt = blockDim.x;
-  const MergeLayout lay(sz);
-  uint64_t* key3 = (uint64_t*)ws;
-  uint32_t* ij3 = (uint32_t*)(key3 + lay.tb);
-  volatile uint8_t* st3 = (volatile uint8_t*)(ij3 + lay.tb);
-  int32_t* owner = (int32_t*)(ws + align_up((size_t)lay.tb * 13, 16));
-  if (tid == 0) {
-    int m3 = 0;
-    for (int nb = 0; nb < kNumNb; nb++) m3 += ((volatile int32_t*)J->kept_count)[nb];
-    s_m3 = m3;
-    s_ns = 0;
-  }
-  __syncthreads();
-  const int m3 = s_m3;
-  {
-    int base = 0;
-    for (int nb = 0; nb < kNumNb; nb++) {
-      const int cnt = ((volatile int32_t*)J->kept_count)[nb];
-      const int off = nb_offset(nb, sz);
-      for (int q = tid; q < cnt; q += nt) {
-        key3[base + q] = ((volatile uint64_t*)J->kept)[2 * (off + q)];
-        ij3[base + q] = (uint32_t)((volatile uint64_t*)J->kept)[2 * (off + q) + 1];
-        st3[base + q] = kUndec;
-      }
-      base += cnt;
+// Split cluster barrier and cluster-scope release/acquire accesses.
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+__device__ __forceinline__ void st_release_cluster(int* p, int v) {
+  asm volatile("st.release.cluster.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire_cluster(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void fence_acquire_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
+
+// Named barriers (ids 1..5) synchronise one warp group without the others.
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ int group_sync_or(int pred, int id, int nthreads) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.s32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(pred), "r"(id), "r"(nthreads)
+      : "memory");
+  return r;
+}
+
+// Stage 2 of one neighbourhood, run by one warp group: greedy independent set
+// of its negative candidates in (delta, block) order with the same-
+// neighbourhood predicate of the reference's GPU merge (mlkernel.cu:51-170
+// after the sort at :256), i.e. the lexicographically-first maximal
+// independent set of the conflict graph.
+//   swap:      rounds of "roots" (no earlier undecided/kept conflicting move)
+//              using per-position tables of the smallest key with an endpoint
+//              there (f_canSwapMerge conflicts are endpoints within 1).
+//   2-opt, Or-opt: conflicts are closed-interval intersections and kept sets
+//              are small: the first alive candidate is kept and its conflicts
+//              removed, repeatedly.
+// On return st[x] == kIn marks the kept candidates.
+__device__ void stage2_group(int nb, int sz, int gtid, int gnt, int bar, Rec* rec, uint64_t* tables,
+                             uint64_t* gmin) {
+  const int m = nb_blocks(nb, sz);
+  if (nb == 0) {
+    uint64_t* minK = tables;
+    uint64_t* minB = tables + (sz + 4);
+    uint64_t* minB2 = tables + 2 * (sz + 4);
+    for (int q = gtid; q < sz + 4; q += gnt) {
+      minK[q] = kKeyNone;
+      minB[q] = kKeyNone;
+      minB2[q] = kKeyNone;
     }
-  }
-  __syncthreads();
-  for (int round = 0; round <= m3; round++) {
-    int any = 0;
-    for (int x = tid; x < m3; x += nt) {
-      if (st3[x] != kUndec) continue;
-      const uint64_t kx = key3[x];
-      const int idx = (int)((kx >> kCtxBits) & 7);
-      const int ix = (int)(ij3[x] & 0xffff), jx = (int)(ij3[x] >> 16);
-      bool out = false, blocked = false;
-      for (int y = 0; y < m3; y++) {
-        const uint64_t ky = key3[y];
-        if (ky >= kx) continue;
-        const uint8_t sy = st3[y];
-        if (sy != kUndec && sy != kIn) continue;
-        const int idy = (int)((ky >> kCtxBits) & 7);
-        if (can_merge(idy, (int)(ij3[y] & 0xffff), (int)(ij3[y] >> 16), idx, ix, jx)) continue;
-        if (sy == kIn) {
-          out = true;
-          break;
+    group_sync(bar, gnt);
+    for (int round = 0; round <= m; round++) {
+      uint64_t* cur = (round & 1) ? minB2 : minB;
+      uint64_t* nxt = (round & 1) ? minB : minB2;
+      for (int x = gtid; x < m; x += gnt) {
+        const Rec r = rec[x];
+        if (r.st != kUndec && r.st != kIn) continue;
+        const int i = (int)(r.ab & 0xffff), j = (int)(r.ab >> 16);
+        amin(&cur[i], r.key);
+        amin(&cur[j], r.key);
+        if (r.st == kIn) {
+          amin(&minK[i], r.key);
+          amin(&minK[j], r.key);
         }
-        blocked = true;
       }
-      if (out) st3[x] = kOut;
-      else if (!blocked) st3[x] = kIn;
-      else any = 1;
+      group_sync(bar, gnt);
+      int any = 0;
+      for (int q = gtid; q < sz + 4; q += gnt) nxt[q] = kKeyNone;
+      for (int x = gtid; x < m; x += gnt) {
+        const Rec r = rec[x];
+        if (r.st != kUndec) continue;
+        const int i = (int)(r.ab & 0xffff), j = (int)(r.ab >> 16);
+        uint64_t qB = kKeyNone, qK = kKeyNone;
+#pragma unroll
+        for (int e = -1; e <= 1; e++) {
+          qB = min(qB, min(cur[i + e], cur[j + e]));
+          qK = min(qK, min(minK[i + e], minK[j + e]));
+        }
+        if (qK < r.key) rec[x].st = kOut;
+        else if (qB >= r.key) rec[x].st = kIn;
+        else any = 1;
+      }
+      if (!group_sync_or(any, bar, gnt)) break;
     }
-    if (!__syncthreads_or(any)) break;
+  } else {
+    const int lane = gtid & 31, gw = gtid >> 5, nw = gnt >> 5;
+    int xs = -1, as = 0, bs = -1;
+    for (int step = 0; step <= m; step++) {
+      uint64_t mk = kKeyNone;
+      constexpr int U = 4;
+      for (int x0 = gtid; x0 < m; x0 += U * gnt) {
+        Rec r[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int x = x0 + u * gnt;
+          if (x < m) r[u] = rec[x];
+          else r[u].st = kNone;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (r[u].st != kUndec) continue;
+          const int x = x0 + u * gnt;
+          if (xs >= 0) {
+            if (x == xs) {
+              rec[x].st = kIn;
+              continue;
+            }
+            const int a = (int)(r[u].ab & 0xffff), b = (int)(r[u].ab >> 16);
+            if (a <= bs && as <= b) {
+              rec[x].st = kOut;
+              continue;
+            }
+          }
+          mk = min(mk, r[u].key);
+        }
+      }
+      mk = warp_min_u64(mk);
+      uint64_t* buf = gmin + (step & 1) * 32;
+      if (lane == 0) buf[gw] = mk;
+      group_sync(bar, gnt);
+      mk = warp_min_u64(lane < nw ? buf[lane] : kKeyNone);
+      if (mk == kKeyNone) break;
+      xs = (int)(mk & ((1u << kCtxBits) - 1));
+      const uint32_t abs_ = rec[xs].ab;
+      as = (int)(abs_ & 0xffff);
+      bs = (int)(abs_ >> 16);
+    }
   }
-  // ---- apply ----
+}
+
+__device__ __forceinline__ int id_of(uint64_t key3) { return (int)((key3 >> kCtxBits) & 7); }
+
+// One cluster of six CTAs per job.  CTAs 0..4 run stage 2 of neighbourhood
+// 0..4 with the whole CTA and hand their kept moves straight to CTA 5 (the
+// leader) through distributed shared memory; the leader, which has fetched the
+// current tour meanwhile, runs stage 3 (cross-neighbourhood greedy with
+// canMerge, mlkernel.cu:649-864 with a stable order), the parallel apply of
+// the selected moves (footprints are disjoint for every pair canMerge
+// accepts), the ADS prefix rebuild and the candidate-key reset.
+template <bool WIDE>
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThreads)
+    k_merge(const JobDev* __restrict__ jobs, int use_smem) {
+  extern __shared__ __align__(16) uint8_t dsm[];
+  __shared__ uint64_t s_gmin[64];  // two step buffers of one entry per warp
+  __shared__ int s_m3, s_ns, s_cnt;
+  __shared__ int s_flag[kNumNb];  // leader: count + 1 published by each stage-2 CTA
+  __shared__ uint32_t s_in[kBitMax / 32], s_und[kBitMax / 32];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const JobDev* J = jobs + blockIdx.x / kClusterCtas;
+  {
+    const int64_t* stt = J->stats;
+    if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;  // the whole cluster
+  }
+  const int sz = J->size, mask = J->nb_mask, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  const MergeLayout lay(sz);
+  // Workspace of this CTA, and the leader's stage-3 lists as seen from here.
+  uint8_t* ws = use_smem ? dsm : (J->ws + (size_t)rank * lay.total);
+  uint8_t* lead = use_smem ? cluster.map_shared_rank(dsm, kClusterCtas - 1)
+                           : (J->ws + (size_t)(kClusterCtas - 1) * lay.total);
+  uint64_t* key3 = (uint64_t*)(lead + lay.o_key3);
+  uint64_t* shp3 = (uint64_t*)(lead + lay.o_shp3);
+  uint32_t* ij3 = (uint32_t*)(lead + lay.o_ij3);
+  volatile uint8_t* st3 = (volatile uint8_t*)(lead + lay.o_st3);
+  int* lead_flags = cluster.map_shared_rank(s_flag, kClusterCtas - 1);
+  int32_t* tour = J->tour;
+  const bool leader = rank == kClusterCtas - 1;
+  int32_t* t_old = (int32_t*)(ws + lay.o_told);
+  int32_t* t_new = (int32_t*)(ws + lay.o_tnew);
+  if (leader) {
+    if (tid < kNumNb) s_flag[tid] = 0;
+    if (tid == 0) s_ns = 0;
+    __syncthreads();
+    cluster_arrive_release();  // the flags are initialised
+    for (int p = tid; p < sz; p += nt) t_old[p] = tour[p];  // completes while stage 2 runs
+  } else {
+    cluster_arrive_relaxed();
+    const int nb = rank;
+    int count = 0;
+    if ((mask >> nb) & 1) {
+      const int m = nb_blocks(nb, sz), off = nb_offset(nb, sz);
+      Rec* rec = (Rec*)ws;
+      uint32_t* ij = (uint32_t*)(ws + lay.o_ij2);
+      const uint64_t* keys = J->keys + off;
+      constexpr int U = 4;
+      for (int x0 = 0; x0 < m; x0 += U * kMergeThreads) {
+        uint64_t kv[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int x = x0 + u * kMergeThreads + tid;
+          kv[u] = x < m ? keys[x] : kKeyNone;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int x = x0 + u * kMergeThreads + tid;
+          if (x >= m) continue;
+          Rec r;
+          r.key = kKeyNone;
+          r.ab = 0;
+          r.st = kNone;
+          if (kv[u] != kKeyNone) {
+            const int64_t cost = key_cost(kv[u], kCtxBits);
+            if (cost < 0) {
+              int i, j;
+              map_move(nb, sz, x, (int)(kv[u] & ((1u << kCtxBits) - 1)), i, j);
+              r.key = make_key(cost, (uint32_t)x, kCtxBits);
+              ij[x] = (uint32_t)i | ((uint32_t)j << 16);
+              if (nb == 0) {
+                r.ab = (uint32_t)i | ((uint32_t)j << 16);
+              } else {
+                int a, b;
+                conflict_interval(nb, i, j, a, b);
+                r.ab = (uint32_t)a | ((uint32_t)b << 16);
+              }
+              r.st = kUndec;
+            }
+          }
+          rec[x] = r;
+        }
+      }
+      if (tid == 0) s_cnt = 0;
+      __syncthreads();
+      stage2_group(nb, sz, tid, nt, 1, rec, (uint64_t*)(ws + lay.o_tab), s_gmin);
+      __syncthreads();
+      // Write the kept moves into this neighbourhood's region of the leader.
+      int nmine = 0;
+      for (int x = tid; x < m; x += nt) nmine += rec[x].st == kIn;
+      int slot = nmine ? atomicAdd(&s_cnt, nmine) : 0;
+      cluster_wait();  // the leader's flags are initialised (arrivals overlap stage 2)
+      const int base = region_off(nb, sz), cap = region_cap(nb, sz);
+      for (int x = tid; x < m; x += nt) {
+        if (rec[x].st != kIn) continue;
+        if (slot < cap) {
+          const uint32_t ijx = ij[x];
+          key3[base + slot] = make_key(key_cost(rec[x].key, kCtxBits), ((uint32_t)nb << kCtxBits) | (uint32_t)x,
+                                       kCtxBits + 3);
+          shp3[base + slot] = move_shape(nb, (int)(ijx & 0xffff), (int)(ijx >> 16));
+          ij3[base + slot] = ijx;
+        }
+        slot++;
+      }
+      fence_acquire_cluster();  // this thread's remote writes, before the flag below
+      __syncthreads();
+      count = min(s_cnt, cap);
+      if (tid == 0 && s_cnt > cap) J->stats[kStatError] = 3;
+    } else {
+      cluster_wait();
+    }
+    if (tid == 0) st_release_cluster(&lead_flags[nb], count + 1);  // publishes the writes above
+    return;
+  }
+  // ---- leader: wait for the five neighbourhoods (bounded), then compact ----
+  if (tid == 0) {
+    long long spins = 0;
+    for (;;) {
+      int ready = 0;
+      for (int nb = 0; nb < kNumNb; nb++) ready += ld_acquire_cluster(&s_flag[nb]) != 0;
+      if (ready == kNumNb) break;
+      if (++spins > (1ll << 26)) {
+        J->stats[kStatError] = 2;
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  __syncthreads();
+  fence_acquire_cluster();
+  if (J->stats[kStatError] == 2) return;
+  {
+    int cnt[kNumNb], cbase[kNumNb + 1];
+    cbase[0] = 0;
+    for (int nb = 0; nb < kNumNb; nb++) {
+      cnt[nb] = s_flag[nb] - 1;
+      cbase[nb + 1] = cbase[nb] + cnt[nb];
+    }
+    // Move every region's entries to the front, chunk by chunk in increasing
+    // order (an entry only moves to a lower index, so unread ones survive).
+    constexpr int V = 4;
+    for (int q0 = 0; q0 < lay.m3cap; q0 += V * nt) {
+      uint64_t kk[V], ss[V];
+      uint32_t jj[V];
+      int dst[V];
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        const int q = q0 + tid + v * nt;
+        dst[v] = -1;
+        if (q >= lay.m3cap) continue;
+        int nb = 0;
+        while (nb + 1 < kNumNb && q >= region_off(nb + 1, sz)) nb++;
+        const int local = q - region_off(nb, sz);
+        if (local >= cnt[nb]) continue;
+        dst[v] = cbase[nb] + local;
+        kk[v] = key3[q];
+        ss[v] = shp3[q];
+        jj[v] = ij3[q];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        if (dst[v] < 0) continue;
+        key3[dst[v]] = kk[v];
+        shp3[dst[v]] = ss[v];
+        ij3[dst[v]] = jj[v];
+        st3[dst[v]] = kUndec;
+      }
+      __syncthreads();
+    }
+    if (tid == 0) s_m3 = cbase[kNumNb];
+    __syncthreads();
+  }
+  const int m3 = s_m3;
+  uint32_t* bits = (uint32_t*)(ws + lay.o_bits);
+  if (m3 <= kBitMax) {
+    // conflict rows: bit y of row x <=> y precedes x and !canMerge(y, x)
+    const int W3 = (m3 + 31) >> 5;
+    for (int x = wid; x < m3; x += nw) {
+      const uint64_t kx = key3[x], sx = shp3[x];
+#pragma unroll 4
+      for (int w = 0; w < W3; w++) {
+        const int y = 32 * w + lane;
+        bool c = false;
+        if (y < m3) c = key3[y] < kx && shapes_conflict(shp3[y], sx);
+        const uint32_t word = __ballot_sync(kFull, c);
+        if (lane == 0) bits[x * W3 + w] = word;
+      }
+    }
+    for (int w = tid; w < W3; w += nt) {
+      s_in[w] = 0;
+      const int rem = m3 - 32 * w;
+      s_und[w] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+    }
+    __syncthreads();
+    for (int round = 0; round <= m3; round++) {
+      int any = 0;
+      for (int x = tid; x < m3; x += nt) {
+        if (st3[x] != kUndec) continue;
+        uint32_t hin = 0, hund = 0;
+        for (int w = 0; w < W3; w++) {
+          const uint32_t r = bits[x * W3 + w];
+          hin |= r & s_in[w];
+          hund |= r & s_und[w];
+        }
+        if (hin) st3[x] = kOut;
+        else if (!hund) st3[x] = kIn;
+        else any = 1;
+      }
+      __syncthreads();
+      for (int w = wid; w < W3; w += nw) {
+        const int x = 32 * w + lane;
+        const uint8_t sx = x < m3 ? st3[x] : kNone;
+        const uint32_t bi = __ballot_sync(kFull, sx == kIn), bu = __ballot_sync(kFull, sx == kUndec);
+        if (lane == 0) {
+          s_in[w] = bi;
+          s_und[w] = bu;
+        }
+      }
+      if (!__syncthreads_or(any)) break;
+    }
+  } else {
+    // long lists: one warp per undecided move scans the earlier ones
+    for (int round = 0; round <= m3; round++) {
+      int any = 0;
+      for (int x = wid; x < m3; x += nw) {
+        if (st3[x] != kUndec) continue;
+        const uint64_t kx = key3[x], sx = shp3[x];
+        bool out = false, blocked = false;
+        for (int y0 = 0; y0 < m3; y0 += 32) {
+          const int y = y0 + lane;
+          bool cin = false, cund = false;
+          if (y < m3) {
+            const uint64_t ky = key3[y];
+            const uint8_t sy = st3[y];
+            if (ky < kx && (sy == kUndec || sy == kIn) && shapes_conflict(shp3[y], sx)) {
+              cin = sy == kIn;
+              cund = sy == kUndec;
+            }
+          }
+          out |= __any_sync(kFull, cin);
+          blocked |= __any_sync(kFull, cund);
+          if (out) break;
+        }
+        if (lane == 0) {
+          if (out) st3[x] = kOut;
+          else if (!blocked) st3[x] = kIn;
+        }
+        if (!out && blocked) any = 1;
+      }
+      if (!__syncthreads_or(any)) break;
+    }
+  }
+  // ---- apply: every position learns which selected move (if any) owns it ----
+  int32_t* owner = (int32_t*)(ws + lay.o_owner);
   for (int p = tid; p < sz; p += nt) owner[p] = -1;
   __syncthreads();
-  const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
   for (int x = wid; x < m3; x += nw) {
     if (st3[x] != kIn) continue;
-    const int id = (int)((key3[x] >> kCtxBits) & 7);
+    const int id = id_of(key3[x]);
     const int i = (int)(ij3[x] & 0xffff), j = (int)(ij3[x] >> 16);
     if (id == 0) {
       if (lane == 0) owner[i] = x;
@@ -586,77 +915,41 @@ __device__ void stage3_apply(const JobDev* J, uint8_t* ws) {
     if (lane == 0) atomicAdd(&s_ns, 1);
   }
   __syncthreads();
-  int32_t* tour = J->tour;
-  int32_t* alt = J->tour_alt;
   for (int p = tid; p < sz; p += nt) {
     const int o = owner[p];
-    int src = p;
-    if (o >= 0) {
-      const int id = (int)((key3[o] >> kCtxBits) & 7);
-      src = move_source(id, (int)(ij3[o] & 0xffff), (int)(ij3[o] >> 16), p);
-    }
-    alt[p] = tour[src];
+    int32_t v = t_old[p];
+    if (o >= 0) v = t_old[move_source(id_of(key3[o]), (int)(ij3[o] & 0xffff), (int)(ij3[o] >> 16), p)];
+    t_new[p] = v;
+    tour[p] = v;
   }
-  __syncthreads();
-  for (int p = tid; p < sz; p += nt) tour[p] = alt[p];
   const int ns = s_ns;
   // Applied moves in (delta, neighbourhood, block) order, for callers that
   // ask for them (the legacy bestNeighbor move vectors).
-  if (J->moves_out != nullptr) {
+  if (J->moves_out != nullptr && (J->flags & kFlagRecordMoves)) {
     for (int x = tid; x < m3; x += nt) {
       if (st3[x] != kIn) continue;
-      int rank = 0;
+      int rank3 = 0;
       for (int y = 0; y < m3; y++)
-        if (st3[y] == kIn && key3[y] < key3[x]) rank++;
-      if (rank < J->moves_cap) {
-        const uint32_t id = (uint32_t)((key3[x] >> kCtxBits) & 7);
+        if (st3[y] == kIn && key3[y] < key3[x]) rank3++;
+      if (rank3 < J->moves_cap) {
+        const uint32_t id = (uint32_t)id_of(key3[x]);
         const uint32_t i = ij3[x] & 0xffff, j = ij3[x] >> 16;
-        J->moves_out[rank] = id | (i << 4) | (j << 18);
-        J->moves_cost[rank] = key_cost(key3[x], kCtxBits + 3);
+        J->moves_out[rank3] = id | (i << 4) | (j << 18);
+        J->moves_cost[rank3] = key_cost(key3[x], kCtxBits + 3);
       }
     }
   }
-  __syncthreads();
   if (tid == 0) {
-    int64_t* stt = J->stats;
-    stt[kStatSweeps] += 1;
-    stt[kStatLastMoves] = ns;
-    stt[kStatMoves] += ns;
-    if (ns > 0) stt[kStatIters] += 1;
-    else stt[kStatConverged] = 1;
-    stt[kStatDone] = 0;
+    unsigned long long* stt = (unsigned long long*)J->stats;
+    atomicAdd(&stt[kStatSweeps], 1ull);
+    atomicExch(&stt[kStatLastMoves], (unsigned long long)ns);
+    atomicAdd(&stt[kStatMoves], (unsigned long long)ns);
+    if (ns > 0) atomicAdd(&stt[kStatIters], 1ull);
+    else atomicExch(&stt[kStatConverged], 1ull);
   }
-  cta_prepare<WIDE>(J);
+  __syncthreads();
+  cta_prepare<WIDE>(J, t_new, t_old);  // t_old is free again: w staging
   cta_reset_keys(J);
-}
-
-template <bool WIDE>
-__global__ void __launch_bounds__(1024) k_merge(const JobDev* __restrict__ jobs, int use_smem) {
-  extern __shared__ __align__(16) uint8_t dsm[];
-  __shared__ int s_cnt, s_last;
-  const int job = blockIdx.x / kNumNb, nb = blockIdx.x % kNumNb;
-  const JobDev* J = jobs + job;
-  {
-    const int64_t* stt = J->stats;
-    if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;
-  }
-  const MergeLayout lay(J->size);
-  uint8_t* ws = use_smem ? dsm : (J->ws + (size_t)nb * lay.total);
-  if ((J->nb_mask >> nb) & 1) {
-    stage2(J, nb, ws, &s_cnt);
-  } else if (threadIdx.x == 0) {
-    J->kept_count[nb] = 0;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned long long prev = atomicAdd((unsigned long long*)&J->stats[kStatDone], 1ull);
-    s_last = prev == (unsigned long long)(kNumNb - 1);
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  stage3_apply<WIDE>(J, ws);
 }
 
 // --------------------------------------------------------------------------
@@ -810,12 +1103,14 @@ template <bool WIDE>
 cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape,
                            cudaStream_t s) {
   switch (shape) {
-    case 0: return sweep_launch<WIDE, 32, 16>(tiles, ntiles, jobs, s);
-    case 1: return sweep_launch<WIDE, 64, 8>(tiles, ntiles, jobs, s);
-    case 2: return sweep_launch<WIDE, 64, 16>(tiles, ntiles, jobs, s);
-    case 3: return sweep_launch<WIDE, 64, 32>(tiles, ntiles, jobs, s);
-    case 4: return sweep_launch<WIDE, 128, 16>(tiles, ntiles, jobs, s);
-    case 5: return sweep_launch<WIDE, 128, 32>(tiles, ntiles, jobs, s);
+    case 0: return sweep_launch<WIDE, 32, 4>(tiles, ntiles, jobs, s);
+    case 1: return sweep_launch<WIDE, 32, 8>(tiles, ntiles, jobs, s);
+    case 2: return sweep_launch<WIDE, 32, 16>(tiles, ntiles, jobs, s);
+    case 3: return sweep_launch<WIDE, 64, 4>(tiles, ntiles, jobs, s);
+    case 4: return sweep_launch<WIDE, 64, 8>(tiles, ntiles, jobs, s);
+    case 5: return sweep_launch<WIDE, 64, 16>(tiles, ntiles, jobs, s);
+    case 6: return sweep_launch<WIDE, 128, 8>(tiles, ntiles, jobs, s);
+    case 7: return sweep_launch<WIDE, 128, 16>(tiles, ntiles, jobs, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -823,14 +1118,25 @@ cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* job
 }  // namespace
 
 size_t merge_smem_bytes(int size) { return MergeLayout(size).total; }
-size_t merge_ws_bytes(int size) { return MergeLayout(size).total * kNumNb; }
-int merge_smem_max_size() { return 2044; }
+size_t merge_ws_bytes(int size) { return MergeLayout(size).total * kClusterCtas; }
+int merge_smem_max_size() {
+  // Largest size whose merge workspace fits the 227 KB opt-in shared memory
+  // (minus the kernel's static shared memory).
+  static int cached = 0;
+  if (cached == 0) {
+    int sz = 8;
+    while (sz < kMaxSize && MergeLayout(sz + 1).total <= (size_t)(227 * 1024 - 4096)) sz++;
+    cached = sz;
+  }
+  return cached;
+}
 
 cudaError_t launch_prepare(const JobDev* jobs, int njobs, bool wide, bool reset_stats,
                            cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
-  if (wide) k_prepare<true><<<njobs, 1024, 0, s>>>(jobs, reset_stats ? 1 : 0);
-  else k_prepare<false><<<njobs, 1024, 0, s>>>(jobs, reset_stats ? 1 : 0);
+  const size_t smem = sizeof(int32_t) * kMaxSize;
+  if (wide) k_prepare<true><<<njobs, 1024, smem, s>>>(jobs, reset_stats ? 1 : 0);
+  else k_prepare<false><<<njobs, 1024, smem, s>>>(jobs, reset_stats ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -842,6 +1148,12 @@ cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs,
 }
 
 cudaError_t configure_merge(size_t bytes) {
+  cudaError_t e0 = cudaFuncSetAttribute(k_prepare<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(sizeof(int32_t) * kMaxSize));
+  if (e0 != cudaSuccess) return e0;
+  e0 = cudaFuncSetAttribute(k_prepare<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(sizeof(int32_t) * kMaxSize));
+  if (e0 != cudaSuccess) return e0;
   cudaError_t e = cudaFuncSetAttribute(k_merge<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_merge<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -851,8 +1163,8 @@ cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem
                          cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
   const size_t smem = use_smem ? MergeLayout(max_size).total : 0;
-  if (wide) k_merge<true><<<njobs * kNumNb, 1024, smem, s>>>(jobs, use_smem ? 1 : 0);
-  else k_merge<false><<<njobs * kNumNb, 1024, smem, s>>>(jobs, use_smem ? 1 : 0);
+  if (wide) k_merge<true><<<njobs * kClusterCtas, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  else k_merge<false><<<njobs * kClusterCtas, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -160,6 +160,24 @@ MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats,
 /* Autotune the sweep tile shape on the current tour; returns the chosen index. */
 MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape);
 
+/* Evaluation without any allocation (no counterpart in the reference).
+ * For callers that cannot allocate device memory -- code running inside
+ * another framework's memory pool or budget, services whose device memory is
+ * partitioned ahead of time, hosts that must not call cudaMalloc/cudaFree
+ * (they synchronise the whole device).  Computes the per-block candidates of
+ * neighbourhood nb (as mlp_solver_eval) for `tour_dev` (n + 1 entries) over
+ * the n x n distances `dist_dev`, writing nb's candidate count of entries to
+ * cost_dev / i_dev / j_dev; every pointer is device memory owned by the
+ * caller.  All intermediate data lives in one fixed 256 KB device array that
+ * the library holds on each GPU it is loaded on until the process exits:
+ * n + 1 <= 2048, larger instances are rejected with MLP_ERR_RANGE.  The first
+ * call on a device looks up that array's address (make it before any stream
+ * capture).  Every call shares the array: calls that overlap on the GPU race,
+ * so serialise them.  Enqueued on `stream` (NULL: legacy default stream). */
+MLP_API int mlp_eval_noalloc(const int32_t* dist_dev, int32_t n, const int32_t* tour_dev, int32_t nb,
+                             int32_t wide, int64_t* cost_dev, int32_t* i_dev, int32_t* j_dev,
+                             void* stream);
+
 /* ---- batched form ---- */
 MLP_API int mlp_batch_create(int32_t wide, mlp_batch_t* out);
 MLP_API void mlp_batch_destroy(mlp_batch_t b);

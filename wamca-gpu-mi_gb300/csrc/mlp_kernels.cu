@@ -1147,6 +1147,14 @@ cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs,
               : sweep_dispatch<false>(tiles, ntiles, jobs, shape, s);
 }
 
+cudaError_t configure_prepare() {
+  cudaError_t e = cudaFuncSetAttribute(k_prepare<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(int32_t) * kMaxSize));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_prepare<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(sizeof(int32_t) * kMaxSize));
+}
+
 cudaError_t configure_merge(size_t bytes) {
   cudaError_t e0 = cudaFuncSetAttribute(k_prepare<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(sizeof(int32_t) * kMaxSize));

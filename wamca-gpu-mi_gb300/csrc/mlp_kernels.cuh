@@ -31,6 +31,8 @@ cudaError_t configure_merge(size_t bytes);
 // nor at its sweep limit (the device-side DVND loop).
 cudaError_t launch_loop_condition(const JobDev* jobs, int njobs, cudaGraphConditionalHandle h,
                                   cudaStream_t s);
+// Opt the ADS-rebuild kernel alone into its dynamic shared memory.
+cudaError_t configure_prepare();
 // Zero the run counters of every job and set its sweep limit.
 cudaError_t launch_stats_begin(const JobDev* jobs, int njobs, int64_t limit, cudaStream_t s);
 cudaError_t launch_prepare(const JobDev* jobs, int njobs, bool wide, bool reset_stats,

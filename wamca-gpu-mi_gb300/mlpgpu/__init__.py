@@ -98,6 +98,7 @@ def lib() -> C.CDLL:
         "mlp_solver_stats": (C.c_int, [vp, P(DvndStats)]),
         "mlp_solver_sweep": (C.c_int, [vp, i32, i32, P(i64)]),
         "mlp_solver_autotune": (C.c_int, [vp, P(i32)]),
+        "mlp_eval_noalloc": (C.c_int, [vp, i32, vp, i32, i32, vp, vp, vp, vp]),
         "mlp_batch_create": (C.c_int, [i32, P(vp)]),
         "mlp_batch_destroy": (None, [vp]),
         "mlp_batch_set_stream": (C.c_int, [vp, vp]),
@@ -312,6 +313,15 @@ class Solver:
         s = C.c_int32()
         _check(lib().mlp_solver_autotune(self._h, C.byref(s)))
         return s.value
+
+
+def eval_noalloc(dist_dev: int, n: int, tour_dev: int, nb: int, wide: bool, cost_dev: int, i_dev: int,
+                 j_dev: int, stream: int = 0) -> None:
+    """mlp_eval_noalloc: per-block candidates of neighbourhood nb computed
+    from caller-owned device buffers, without any allocation."""
+    _check(lib().mlp_eval_noalloc(C.c_void_p(dist_dev), n, C.c_void_p(tour_dev), nb, int(wide),
+                                  C.c_void_p(cost_dev), C.c_void_p(i_dev), C.c_void_p(j_dev),
+                                  C.c_void_p(stream)))
 
 
 class Batch:

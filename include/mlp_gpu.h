@@ -53,7 +53,9 @@ enum {
   MLP_ERR_FORMAT = 5,      /* malformed or unsupported instance file */
   MLP_ERR_NOMEM = 6,       /* device or host allocation failed / over budget */
   MLP_ERR_STATE = 7,       /* call not valid in the handle's current state */
-  MLP_ERR_UNSUPPORTED = 8  /* feature the reference does not support */
+  MLP_ERR_UNSUPPORTED = 8, /* feature the reference does not support */
+  MLP_ERR_CANCELLED = 9,   /* served request cancelled before it finished */
+  MLP_PENDING = 10         /* served request not finished yet (not an error) */
 };
 
 enum { MLP_NB_SWAP = 0, MLP_NB_2OPT = 1, MLP_NB_OROPT1 = 2, MLP_NB_OROPT2 = 3, MLP_NB_OROPT3 = 4 };
@@ -195,6 +197,56 @@ MLP_API int mlp_batch_reset(mlp_batch_t b);
 MLP_API int mlp_batch_result(mlp_batch_t b, int32_t job, int32_t* tour, int32_t len,
                              mlp_dvnd_stats_t* stats);
 MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape);
+
+/* ---- serving form: continuous batching of arriving searches ----
+ * A server owns a CUDA stream and a device memory pool.  Requests (instance
+ * coordinates, start tour, neighbourhood mask, sweep limit) are queued by
+ * mlp_server_submit; each mlp_server_step admits queued requests in arrival
+ * order while a slot is free and their footprint (mlp_server_footprint: the
+ * n x n int32 distances, coordinates, tour and ADS arrays) fits the memory
+ * budget, runs `iters` DVND iterations over every admitted search in shared
+ * launches and retires the searches that converged or used their sweep limit.
+ * A search's result is the same as mlp_solver_dvnd's on the same input, alone
+ * or in any mix.  submit / finished / result / cancel / status may be called
+ * from other threads while one thread calls step. */
+typedef struct {
+  double arrival;   /* seconds on the server clock (mlp_server_now) */
+  double admitted;  /* admission time (-1 if never admitted) */
+  double finished;  /* time the result became available */
+  int32_t status;   /* MLP_OK, MLP_ERR_CANCELLED or the error that ended it */
+  int32_t n;
+} mlp_serve_info_t;
+
+/* memory_budget: device bytes for admitted searches; max_active: slots. */
+MLP_API int mlp_server_create(int64_t memory_budget, int32_t wide, int32_t max_active, mlp_server_t* out);
+MLP_API void mlp_server_destroy(mlp_server_t s);
+/* Seconds since the server was created (the clock of arrival/finish times). */
+MLP_API double mlp_server_now(mlp_server_t s);
+/* Device bytes one search of n nodes is admitted against (-1: n invalid). */
+MLP_API int64_t mlp_server_footprint(int32_t n, int32_t wide);
+/* Fixed tile shape for the sweeps (-1: chosen per step). */
+MLP_API int mlp_server_set_tile_shape(mlp_server_t s, int32_t shape);
+/* Queues a search of the EUC_2D instance (x, y) from `tour` (n + 1 entries).
+ * arrival < 0 stamps the current server time.  Rejected with MLP_ERR_NOMEM if
+ * its footprint exceeds the whole budget, MLP_ERR_ARG for a malformed tour. */
+MLP_API int mlp_server_submit(mlp_server_t s, int32_t n, const int32_t* x, const int32_t* y, int32_t dist_round,
+                              const int32_t* tour, int32_t len, int32_t nb_mask, int32_t max_iters,
+                              double arrival, int64_t* id);
+/* Admits, iterates `iters` times, retires; reports the active and queued counts. */
+MLP_API int mlp_server_step(mlp_server_t s, int32_t iters, int32_t* active, int32_t* queued);
+/* Ids finished since the last call (at most cap of them). */
+MLP_API int mlp_server_finished(mlp_server_t s, int64_t* ids, int32_t cap, int32_t* count);
+/* Takes a finished request's result (tour may be NULL); MLP_PENDING while it
+ * is queued or running. */
+MLP_API int mlp_server_result(mlp_server_t s, int64_t id, int32_t* tour, int32_t len, mlp_dvnd_stats_t* stats,
+                              mlp_serve_info_t* info);
+/* Cancels a queued request at once, a running one at the end of the next step. */
+MLP_API int mlp_server_cancel(mlp_server_t s, int64_t id);
+MLP_API int mlp_server_status(mlp_server_t s, int64_t* mem_in_use, int32_t* active, int32_t* queued,
+                              int32_t* finished);
+/* Failure injection on the host: the next `count` admissions fail as if a
+ * host allocation had failed (their requests end with MLP_ERR_NOMEM). */
+MLP_API int mlp_server_fail_next_admissions(mlp_server_t s, int32_t count);
 
 #ifdef __cplusplus
 }

@@ -110,6 +110,8 @@ MLP_API const char* mlp_status_string(int status) {
     case MLP_ERR_NOMEM: return "out of memory";
     case MLP_ERR_STATE: return "invalid state";
     case MLP_ERR_UNSUPPORTED: return "unsupported";
+    case MLP_ERR_CANCELLED: return "cancelled";
+    case MLP_PENDING: return "pending";
     default: return "unknown status";
   }
 }

@@ -36,6 +36,12 @@ int cuda_status(cudaError_t e, const char* what) {
 
 // ---------------------------------------------------------------- Problem
 Problem::~Problem() {
+  if (async_alloc) {
+    if (dD) cudaFreeAsync(dD, alloc_stream);
+    if (dX) cudaFreeAsync(dX, alloc_stream);
+    if (dY) cudaFreeAsync(dY, alloc_stream);
+    return;
+  }
   if (dD) cudaFree(dD);
   if (dX) cudaFree(dX);
   if (dY) cudaFree(dY);
@@ -94,6 +100,44 @@ int problem_from_coords(int n, const int32_t* x, const int32_t* y, int cost_tour
     set_error("a distance exceeds 65535 (the reference stores weights as ushort)");
     return kErrRange;
   }
+  *out = p.release();
+  return kOk;
+}
+
+int problem_from_coords_async(int n, const int32_t* x, const int32_t* y, int dist_round, cudaMemPool_t pool,
+                              cudaStream_t stream, Problem** out) {
+  if (!x || !y || !out) {
+    set_error("null argument");
+    return kErrArg;
+  }
+  int st = check_n(n, 1);
+  if (st != kOk) return st;
+  const auto mmx = std::minmax_element(x, x + n);
+  const auto mmy = std::minmax_element(y, y + n);
+  if ((int64_t)*mmx.second - *mmx.first > 32767 || (int64_t)*mmy.second - *mmy.first > 32767) {
+    // spans <= 32767 also bound every distance by 46341 < 65535
+    set_error("coordinate spans must not exceed 32767 so that dx*dx + dy*dy fits int32");
+    return kErrRange;
+  }
+  std::unique_ptr<Problem> p(new Problem());
+  p->n = n;
+  p->size = n + 1;
+  p->cost_tour = 1;
+  p->dist_round = dist_round ? 1 : 0;
+  p->alloc_stream = stream;
+  p->async_alloc = true;
+  p->dmax = 46341;
+  MLP_CUDA(cudaGetDevice(&p->device), "cudaGetDevice");
+  MLP_CUDA(cudaMallocFromPoolAsync(&p->dX, sizeof(int32_t) * n, pool, stream), "cudaMallocAsync(coords)");
+  MLP_CUDA(cudaMallocFromPoolAsync(&p->dY, sizeof(int32_t) * n, pool, stream), "cudaMallocAsync(coords)");
+  MLP_CUDA(cudaMallocFromPoolAsync(&p->dD, sizeof(int32_t) * (size_t)n * n + 16, pool, stream),
+           "cudaMallocAsync(D)");
+  // Pageable sources: the copies are staged before the calls return.
+  MLP_CUDA(cudaMemcpyAsync(p->dX, x, sizeof(int32_t) * n, cudaMemcpyHostToDevice, stream), "copy coords");
+  MLP_CUDA(cudaMemcpyAsync(p->dY, y, sizeof(int32_t) * n, cudaMemcpyHostToDevice, stream), "copy coords");
+  int32_t* dmax = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(p->dD) + sizeof(int32_t) * (size_t)n * n);
+  MLP_CUDA(cudaMemsetAsync(dmax, 0, sizeof(int32_t), stream), "memset");
+  MLP_CUDA(launch_dist(p->dX, p->dY, n, p->dist_round, p->dD, dmax, stream), "dist kernel");
   *out = p.release();
   return kOk;
 }
@@ -220,20 +264,42 @@ size_t job_bytes(int size, bool wide, int moves_cap) {
 }
 
 Job::~Job() {
-  if (arena) cudaFree(arena);
+  if (!arena) return;
+  if (async_alloc) cudaFreeAsync(arena, alloc_stream);
+  else cudaFree(arena);
 }
+
+static void job_layout(Job* j, Problem* p, bool wide, int moves_cap);
 
 int job_create(Problem* p, bool wide, int moves_cap, Job** out) {
   std::unique_ptr<Job> j(new Job());
+  j->arena_bytes = job_bytes(p->size, wide, moves_cap);
+  MLP_CUDA(cudaMalloc(&j->arena, j->arena_bytes), "cudaMalloc(job)");
+  MLP_CUDA(cudaMemset(j->arena, 0, j->arena_bytes), "memset(job)");
+  job_layout(j.get(), p, wide, moves_cap);
+  *out = j.release();
+  return kOk;
+}
+
+int job_create_async(Problem* p, bool wide, cudaMemPool_t pool, cudaStream_t stream, Job** out) {
+  std::unique_ptr<Job> j(new Job());
+  j->arena_bytes = job_bytes(p->size, wide, 0);
+  j->alloc_stream = stream;
+  j->async_alloc = true;
+  MLP_CUDA(cudaMallocFromPoolAsync(&j->arena, j->arena_bytes, pool, stream), "cudaMallocAsync(job)");
+  MLP_CUDA(cudaMemsetAsync(j->arena, 0, j->arena_bytes, stream), "memset(job)");
+  job_layout(j.get(), p, wide, 0);
+  *out = j.release();
+  return kOk;
+}
+
+static void job_layout(Job* j, Problem* p, bool wide, int moves_cap) {
   j->prob = p;
   j->wide = wide;
   j->size = p->size;
   j->moves_cap = moves_cap;
   const int size = p->size;
   const size_t pad = size + 8, tb = total_blocks(size), cw = wide ? 8 : 4;
-  j->arena_bytes = job_bytes(size, wide, moves_cap);
-  MLP_CUDA(cudaMalloc(&j->arena, j->arena_bytes), "cudaMalloc(job)");
-  MLP_CUDA(cudaMemset(j->arena, 0, j->arena_bytes), "memset(job)");
   char* c = static_cast<char*>(j->arena);
   JobDev& d = j->dev;
   d.D = p->dD;
@@ -259,8 +325,13 @@ int job_create(Problem* p, bool wide, int moves_cap, Job** out) {
   d.size = size;
   d.nb_mask = 0x1f;
   d.flags = wide ? kFlagWide : 0;
-  *out = j.release();
-  return kOk;
+}
+
+void job_tiles(int size, int shape, std::vector<SweepTile>* out) {
+  const TileShape ts = kTileShapes[shape];
+  out->clear();
+  for (int r0 = 1; r0 <= size - 3; r0 += ts.tr)
+    for (int L0 = 1; r0 + L0 <= size - 2; L0 += ts.tl) out->push_back(SweepTile{0, r0, L0, 0});
 }
 
 int default_shape(int size) {
@@ -271,7 +342,7 @@ int default_shape(int size) {
 
 // ---------------------------------------------------------------- JobSet
 JobSet::JobSet(std::vector<Job*> jobs, bool wide, cudaStream_t stream)
-    : jobs_(std::move(jobs)), wide_(wide), stream_(stream) {}
+    : all_jobs_(jobs), jobs_(std::move(jobs)), wide_(wide), stream_(stream) {}
 
 JobSet::~JobSet() {
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
@@ -317,7 +388,9 @@ int JobSet::init() {
     jobs_[q]->dev.stats = dstats_ + q * kStatWords;
     h[q] = jobs_[q]->dev;
   }
-  MLP_CUDA(cudaMemcpy(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice), "copy jobs");
+  MLP_CUDA(cudaMemcpyAsync(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice, stream_),
+           "copy jobs");
+  MLP_CUDA(cudaStreamSynchronize(stream_), "copy jobs");
   if (shape_ < 0) shape_ = default_shape(max_size_);
   return build_tiles();
 }
@@ -341,6 +414,33 @@ int JobSet::build_tiles() {
   MLP_CUDA(cudaMemcpy(dtiles_, tiles.data(), sizeof(SweepTile) * tiles.size(), cudaMemcpyHostToDevice),
            "copy tiles");
   return kOk;
+}
+
+int JobSet::set_active(const std::vector<int>& idx) {
+  std::vector<Job*> next;
+  for (int q : idx) {
+    if (q < 0 || q >= (int)all_jobs_.size()) {
+      set_error("active job index out of range");
+      return kErrArg;
+    }
+    next.push_back(all_jobs_[q]);
+  }
+  if (next == jobs_) return kOk;
+  jobs_ = next;
+  if (jobs_.empty()) return kOk;
+  std::vector<JobDev> h(jobs_.size());
+  for (size_t q = 0; q < jobs_.size(); q++) h[q] = jobs_[q]->dev;
+  MLP_CUDA(cudaMemcpyAsync(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice, stream_),
+           "copy jobs");
+  MLP_CUDA(cudaStreamSynchronize(stream_), "copy jobs");
+  return build_tiles();
+}
+
+int JobSet::ensure_all_active() {
+  if (jobs_.size() == all_jobs_.size()) return kOk;
+  std::vector<int> all(all_jobs_.size());
+  for (size_t q = 0; q < all.size(); q++) all[q] = (int)q;
+  return set_active(all);
 }
 
 int JobSet::set_stream(cudaStream_t s) {
@@ -376,6 +476,10 @@ int JobSet::set_mask(int mask) {
     return kErrArg;
   }
   if (mask == mask_) return kOk;
+  {
+    int st = ensure_all_active();
+    if (st != kOk) return st;
+  }
   mask_ = mask;
   for (size_t q = 0; q < jobs_.size(); q++) {
     jobs_[q]->dev.nb_mask = mask;
@@ -388,6 +492,10 @@ int JobSet::set_mask(int mask) {
 }
 
 int JobSet::set_record_moves(bool on) {
+  {
+    int st = ensure_all_active();
+    if (st != kOk) return st;
+  }
   for (size_t q = 0; q < jobs_.size(); q++) {
     int32_t f = jobs_[q]->dev.flags;
     f = on ? (f | kFlagRecordMoves) : (f & ~kFlagRecordMoves);
@@ -402,6 +510,10 @@ int JobSet::set_record_moves(bool on) {
 }
 
 int JobSet::prepare(bool reset_stats) {
+  {
+    int st = ensure_all_active();
+    if (st != kOk) return st;
+  }
   MLP_CUDA(launch_prepare(djobs_, (int)jobs_.size(), wide_, reset_stats, stream_), "prepare kernel");
   return kOk;
 }
@@ -413,6 +525,10 @@ int JobSet::launch_iteration() {
 }
 
 int JobSet::sweep_only() {
+  {
+    int st = ensure_all_active();
+    if (st != kOk) return st;
+  }
   MLP_CUDA(launch_stats_begin(djobs_, (int)jobs_.size(), 1, stream_), "stats kernel");
   MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
   return kOk;
@@ -535,38 +651,59 @@ int JobSet::run(int max_iters, bool sync) {
     set_error("max_iters must be positive");
     return kErrArg;
   }
-  if (device_loop_ && stream_ != 0) {
+  {
+    int st = ensure_all_active();
+    if (st != kOk) return st;
+  }
+  if (device_loop_ && stream_ != 0 && all_jobs_.size() == 1) {
     int st = enqueue_device_loop(max_iters);
     if (st != kOk || !sync) return st;
     std::vector<std::array<int64_t, kStatWords>> s;
     return read_stats(&s);
   }
   MLP_CUDA(launch_stats_begin(djobs_, (int)jobs_.size(), max_iters, stream_), "stats kernel");
+  // Host-checked loop.  A single job replays CUDA graphs of `unroll`
+  // iterations; a batch launches directly and, after every check, drops the
+  // jobs that converged from the launches (grids shrink as the batch drains).
+  const bool graphs = all_jobs_.size() == 1 && stream_ != 0;
+  std::vector<int> active(all_jobs_.size());
+  for (size_t q = 0; q < active.size(); q++) active[q] = (int)q;
   int done = 0;
+  int st = kOk;
   while (done < max_iters) {
     const int u = std::min(unroll_, max_iters - done);
-    int st = enqueue_iterations(u);
-    if (st != kOk) return st;
+    if (graphs) {
+      st = enqueue_iterations(u);
+    } else {
+      for (int q = 0; q < u && st == kOk; q++) st = launch_iteration();
+    }
+    if (st != kOk) break;
     done += u;
     if (!sync && done < max_iters) continue;
     std::vector<std::array<int64_t, kStatWords>> s;
     st = read_stats(&s);
-    if (st != kOk) return st;
-    bool all = true;
-    for (auto& a : s)
-      if (!a[kStatConverged] && a[kStatSweeps] < max_iters) all = false;
-    if (all) break;
+    if (st != kOk) break;
+    std::vector<int> next;
+    for (int q : active)
+      if (!s[q][kStatConverged] && s[q][kStatSweeps] < max_iters) next.push_back(q);
+    if (next.empty()) break;
+    if (!graphs && next.size() < active.size()) {
+      st = set_active(next);
+      if (st != kOk) break;
+      active.swap(next);
+    }
   }
-  return kOk;
+  const int st2 = ensure_all_active();
+  return st != kOk ? st : st2;
 }
 
 int JobSet::read_stats(std::vector<std::array<int64_t, kStatWords>>* out) {
-  MLP_CUDA(cudaMemcpyAsync(hstats_, dstats_, sizeof(int64_t) * kStatWords * jobs_.size(),
+  MLP_CUDA(cudaMemcpyAsync(hstats_, dstats_, sizeof(int64_t) * kStatWords * all_jobs_.size(),
                            cudaMemcpyDeviceToHost, stream_),
            "read stats");
   MLP_CUDA(cudaStreamSynchronize(stream_), "read stats");
-  out->resize(jobs_.size());
-  for (size_t q = 0; q < jobs_.size(); q++)
+  out->resize(all_jobs_.size());
+  for (size_t q = 0; q < all_jobs_.size(); q++)
     std::memcpy((*out)[q].data(), hstats_ + q * kStatWords, sizeof(int64_t) * kStatWords);
   int64_t err = 0;
   for (auto& a : *out) err |= a[kStatError];
@@ -578,7 +715,7 @@ int JobSet::read_stats(std::vector<std::array<int64_t, kStatWords>>* out) {
 }
 
 int64_t JobSet::evals_per_sweep(int job, int mask) const {
-  const int sz = jobs_[job]->size;
+  const int sz = all_jobs_[job]->size;
   int64_t e = 0;
   for (int nb = 0; nb < kNumNb; nb++)
     if ((mask >> nb) & 1) e += (int64_t)nb_blocks(nb, sz) * nb_threads(nb, sz);

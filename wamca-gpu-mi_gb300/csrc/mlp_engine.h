@@ -52,11 +52,17 @@ struct Problem {
   int32_t* dY = nullptr;
   std::vector<int32_t> hx, hy;
   std::string name;
+  cudaStream_t alloc_stream = nullptr;  // non-null: stream-ordered allocation
+  bool async_alloc = false;
   ~Problem();
 };
 
 int problem_from_coords(int n, const int32_t* x, const int32_t* y, int cost_tour, int dist_round,
                         bool x_on_device, Problem** out);
+// Same with stream-ordered allocation from `pool` and no host
+// synchronisation (the coordinates are staged before the call returns).
+int problem_from_coords_async(int n, const int32_t* x, const int32_t* y, int dist_round, cudaMemPool_t pool,
+                              cudaStream_t stream, Problem** out);
 int problem_from_matrix(int n, const int32_t* D, int cost_tour, bool on_device, Problem** out);
 int problem_from_tsplib(const char* path, int cost_tour, int dist_round, Problem** out);
 // TSPLIB EUC_2D reader (coordinates rounded with TSPLIB nint, source/tsplib.cpp:237-240).
@@ -72,10 +78,16 @@ struct Job {
   size_t arena_bytes = 0;
   JobDev dev{};           // host copy of the descriptor
   int moves_cap = 0;
+  cudaStream_t alloc_stream = nullptr;
+  bool async_alloc = false;
   ~Job();
 };
 
 int job_create(Problem* p, bool wide, int moves_cap, Job** out);
+// Stream-ordered variant (memory from `pool`).
+int job_create_async(Problem* p, bool wide, cudaMemPool_t pool, cudaStream_t stream, Job** out);
+// Per-job sweep tiles of one tile shape (job index 0).
+void job_tiles(int size, int shape, std::vector<SweepTile>* out);
 size_t job_bytes(int size, bool wide, int moves_cap);
 
 struct DvndResult {
@@ -122,15 +134,21 @@ class JobSet {
   int enqueue_device_loop(int max_iters);
   int read_stats(std::vector<std::array<int64_t, kStatWords>>* out);
   int64_t evals_per_sweep(int job, int mask) const;
-  const std::vector<Job*>& jobs() const { return jobs_; }
+  const std::vector<Job*>& jobs() const { return all_jobs_; }
+  // Launch only the listed jobs (indices into jobs()); converged jobs are
+  // dropped this way between graph replays of a batch.
+  int set_active(const std::vector<int>& idx);
+  int ensure_all_active();
   JobDev* device_jobs() const { return djobs_; }
   int ntiles() const { return ntiles_; }
+  // One DVND iteration over the current jobs (no statistics reset).
+  int launch_iteration();
 
  private:
   int build_tiles();
   int graph_for(int iters, cudaGraphExec_t* out);
-  int launch_iteration();
-  std::vector<Job*> jobs_;
+  std::vector<Job*> all_jobs_;  // every job of the set (statistics order)
+  std::vector<Job*> jobs_;      // the jobs the launches cover
   bool wide_;
   cudaStream_t stream_;
   int shape_ = -1;

@@ -1162,6 +1162,10 @@ cudaError_t configure_merge(size_t bytes) {
   e0 = cudaFuncSetAttribute(k_prepare<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(sizeof(int32_t) * kMaxSize));
   if (e0 != cudaSuccess) return e0;
+  // The attribute is a per-device upper bound shared by every job set of the
+  // process: never lower it below the largest shared-memory merge layout, or
+  // a set configured earlier with larger jobs would fail its next launch.
+  bytes = bytes > MergeLayout(merge_smem_max_size()).total ? bytes : MergeLayout(merge_smem_max_size()).total;
   cudaError_t e = cudaFuncSetAttribute(k_merge<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_merge<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);

@@ -48,6 +48,20 @@ class DvndStats(C.Structure):
         return {f: int(getattr(self, f)) for f, _ in self._fields_ if f != "reserved"}
 
 
+class ServeInfo(C.Structure):
+    _fields_ = [
+        ("arrival", C.c_double),
+        ("admitted", C.c_double),
+        ("finished", C.c_double),
+        ("status", C.c_int32),
+        ("n", C.c_int32),
+    ]
+
+
+PENDING = 10
+CANCELLED = 9
+
+
 _lib: Optional[C.CDLL] = None
 
 
@@ -107,6 +121,18 @@ def lib() -> C.CDLL:
         "mlp_batch_run": (C.c_int, [vp, i32, i32]),
         "mlp_batch_reset": (C.c_int, [vp]),
         "mlp_batch_result": (C.c_int, [vp, i32, vp, i32, P(DvndStats)]),
+        "mlp_server_create": (C.c_int, [i64, i32, i32, P(vp)]),
+        "mlp_server_destroy": (None, [vp]),
+        "mlp_server_now": (C.c_double, [vp]),
+        "mlp_server_footprint": (i64, [i32, i32]),
+        "mlp_server_set_tile_shape": (C.c_int, [vp, i32]),
+        "mlp_server_submit": (C.c_int, [vp, i32, vp, vp, i32, vp, i32, i32, i32, C.c_double, P(i64)]),
+        "mlp_server_step": (C.c_int, [vp, i32, P(i32), P(i32)]),
+        "mlp_server_finished": (C.c_int, [vp, P(i64), i32, P(i32)]),
+        "mlp_server_result": (C.c_int, [vp, i64, vp, i32, P(DvndStats), P(ServeInfo)]),
+        "mlp_server_cancel": (C.c_int, [vp, i64]),
+        "mlp_server_status": (C.c_int, [vp, P(i64), P(i32), P(i32), P(i32)]),
+        "mlp_server_fail_next_admissions": (C.c_int, [vp, i32]),
         "bestNeighborSimple": (C.c_uint, [C.c_char_p, vp, C.c_uint, C.c_int]),
         "bestNeighbor": (C.c_uint, [C.c_char_p, vp, C.c_uint, C.c_int, C.c_bool, C.c_uint, vp, vp, vp,
                                     vp, vp, C.c_bool, C.c_uint, vp]),
@@ -372,6 +398,82 @@ class Batch:
         st = DvndStats()
         _check(lib().mlp_batch_result(self._h, job, _ptr(t), len(t), C.byref(st)))
         return t, st.as_dict()
+
+
+class Server:
+    """Serving form: continuous batching of DVND searches that arrive over time.
+
+    submit() queues a search; step() admits queued searches while slots and the
+    memory budget allow, runs `iters` DVND iterations over every admitted search
+    in shared launches and retires the finished ones; finished() lists the ids
+    that completed and result() takes one result.
+    """
+
+    def __init__(self, memory_budget: int, wide: bool = False, max_active: int = 512):
+        self._h = C.c_void_p()
+        _check(lib().mlp_server_create(int(memory_budget), int(wide), int(max_active), C.byref(self._h)))
+        self.wide = wide
+
+    def close(self) -> None:
+        if self._h:
+            lib().mlp_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def footprint(n: int, wide: bool = False) -> int:
+        return int(lib().mlp_server_footprint(n, int(wide)))
+
+    def now(self) -> float:
+        return float(lib().mlp_server_now(self._h))
+
+    def set_tile_shape(self, shape: int) -> None:
+        _check(lib().mlp_server_set_tile_shape(self._h, shape))
+
+    def submit(self, x, y, tour, dist_round: bool = True, nb_mask: int = NB_ALL, max_iters: int = 1 << 20,
+               arrival: float = -1.0) -> int:
+        x, y, t = _i32(x), _i32(y), _i32(tour)
+        rid = C.c_int64()
+        _check(lib().mlp_server_submit(self._h, len(x), _ptr(x), _ptr(y), int(dist_round), _ptr(t), len(t),
+                                       nb_mask, max_iters, float(arrival), C.byref(rid)))
+        return rid.value
+
+    def step(self, iters: int = 1):
+        a, q = C.c_int32(), C.c_int32()
+        _check(lib().mlp_server_step(self._h, iters, C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def finished(self, cap: int = 4096) -> list:
+        ids = (C.c_int64 * cap)()
+        k = C.c_int32()
+        _check(lib().mlp_server_finished(self._h, ids, cap, C.byref(k)))
+        return [int(ids[i]) for i in range(k.value)]
+
+    def result(self, rid: int, n: int):
+        """(tour, stats, info) of a finished request, or None while pending."""
+        t = np.zeros(n + 1, np.int32)
+        st, info = DvndStats(), ServeInfo()
+        s = lib().mlp_server_result(self._h, rid, _ptr(t), len(t), C.byref(st), C.byref(info))
+        if s == PENDING:
+            return None
+        _check(s)
+        return t, st.as_dict(), {f: getattr(info, f) for f, _ in info._fields_}
+
+    def cancel(self, rid: int) -> None:
+        _check(lib().mlp_server_cancel(self._h, rid))
+
+    def status(self) -> dict:
+        m, a, q, f = C.c_int64(), C.c_int32(), C.c_int32(), C.c_int32()
+        _check(lib().mlp_server_status(self._h, C.byref(m), C.byref(a), C.byref(q), C.byref(f)))
+        return {"mem_in_use": m.value, "active": a.value, "queued": q.value, "finished": f.value}
+
+    def fail_next_admissions(self, count: int) -> None:
+        _check(lib().mlp_server_fail_next_admissions(self._h, count))
 
 
 class Legacy:

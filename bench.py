@@ -14,6 +14,13 @@ Reported:
   roofline   the sweep kernel: algorithmic bytes per sweep / CUDA-event time
   cpu_baseline  the oracle (CPU restatement of the reference path) on the
              host cores, on a bounded sample of the same workload
+Beside the headline, in the same line:
+  batched    512 clustered instances (n log-uniform [100,1000]) x 4 starts in
+             one batch: solves/s against the plain form on a sample
+  serving    an open-loop Poisson request stream (n log-uniform [50,2000]) at
+             several offered rates: solves/s, p50/p99 latency, 40 GB budget
+  large      n = 10000 with int64 costs: a 2-opt + Or-opt-3 sweep and a DVND
+             capped in sweeps
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -238,6 +245,291 @@ def run_reference(args, world, rank) -> None:
 
 
 # --------------------------------------------------------------------------- GPU
+def _events(k):
+    import torch
+
+    return [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+
+
+def _pct(vals, q):
+    v = sorted(vals)
+    return v[min(len(v) - 1, max(0, math.ceil(q * len(v)) - 1))] if v else None
+
+
+def time_sweep(mlpgpu, solver, stream, flush, mask, reps):
+    """Median CUDA-event time of one sweep kernel launch (seconds).
+
+    mlp_solver_sweep(mask, R) enqueues a stats reset, R sweep kernels and a
+    prepare; the R = 0 call is timed too and subtracted.
+    """
+    import torch
+
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            solver.sweep(mask, 1)
+    a, b, c, d = _events(reps), _events(reps), _events(reps), _events(reps)
+    with torch.cuda.stream(stream):
+        for r in range(reps):
+            flush.zero_()
+            a[r].record(stream)
+            solver.sweep(mask, 1)
+            b[r].record(stream)
+        for r in range(reps):
+            flush.zero_()
+            c[r].record(stream)
+            solver.sweep(mask, 0)
+            d[r].record(stream)
+    torch.cuda.synchronize()
+    t1 = statistics.median(x.elapsed_time(y) for x, y in zip(a, b)) * 1e-3
+    t0 = statistics.median(x.elapsed_time(y) for x, y in zip(c, d)) * 1e-3
+    return max(t1 - t0, 1e-9)
+
+
+def plain_launches(sweeps: int, unroll: int = 16) -> int:
+    """Kernels one mlp_solver_dvnd enqueues (host-checked loop): prepare of the
+    new tour, statistics reset, then graphs of `unroll` iterations of
+    (sweep, merge) until the check after a graph sees convergence."""
+    return 2 + 2 * unroll * math.ceil(max(sweeps, 1) / unroll)
+
+
+def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
+    """configs[1]: plain single instance, n = 1000 (the headline)."""
+    import torch
+
+    n = N_NODES
+    size = n + 1
+    x, y = workloads.uniform_instance(n, INSTANCE_SEED)
+    prob = mlpgpu.Problem.from_coords(x, y, dist_round=True)
+    solver = mlpgpu.Solver(prob, wide=False)
+    solver.set_stream(stream.cuda_stream)
+    nsteps = args.warmup + args.steps
+    tours = [workloads.random_perm_tour(n, 1_000 * rank + k) for k in range(nsteps)]
+    tours_dev = torch.tensor(np.stack(tours), dtype=torch.int32, device="cuda")
+    solver.set_tour(tours[0])
+    shape = solver.autotune() if args.autotune else None
+    t_sweep = time_sweep(mlpgpu, solver, stream, flush, mlpgpu.NB_ALL, args.sweeps)
+
+    # DVND steps: device time, start tours already resident in HBM, L2 flushed.
+    step_ms, step_evals, step_sweeps, costs = [], [], [], []
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    for k in range(nsteps):
+        if k == args.warmup:
+            sampler.start()
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+        e0, e1 = _events(2)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            solver.set_tour_device(tours_dev[k].data_ptr())
+            st = solver.dvnd(mlpgpu.NB_ALL)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            step_ms.append(e0.elapsed_time(e1))
+            step_evals.append(st["evals"])
+            step_sweeps.append(st["sweeps"])
+            costs.append(st["cost"])
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+
+    # e2e through the C-ABI with host buffers (H2D start tour, D2H result).
+    host_tours = [torch.from_numpy(t).pin_memory() for t in tours]
+    out = torch.empty(size, dtype=torch.int32).pin_memory()
+    e2e_s, e2e_evals = [], []
+    L = mlpgpu.lib()
+    for k in range(nsteps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mlpgpu._check(L.mlp_solver_set_tour(solver._h, mlpgpu.C.c_void_p(host_tours[k].data_ptr()), size))
+        st = mlpgpu.DvndStats()
+        mlpgpu._check(L.mlp_solver_dvnd(solver._h, mlpgpu.NB_ALL, 1 << 20, mlpgpu.C.byref(st)))
+        mlpgpu._check(L.mlp_solver_get_tour(solver._h, mlpgpu.C.c_void_p(out.data_ptr()), size))
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            e2e_s.append(dt)
+            e2e_evals.append(st.evals)
+            assert st.cost == costs[k - args.warmup], "e2e and device runs disagree"
+    return {
+        "n": n, "size": size, "t_sweep": t_sweep, "shape": shape, "step_ms": step_ms, "step_evals": step_evals,
+        "step_sweeps": step_sweeps, "costs": costs, "clocks": clocks, "e2e_s": e2e_s, "e2e_evals": e2e_evals,
+    }
+
+
+def bench_batched(args, mlpgpu, workloads, stream):
+    """configs[2]: 512 clustered instances, n log-uniform in [100, 1000], 4
+    seeded random starts each (2048 DVND searches) in one batch, against the
+    plain form (one mlp_solver_dvnd per search) on a sample of the searches."""
+    import torch
+
+    ninst, starts = args.batch_instances, 4
+    sizes = workloads.log_uniform_sizes(ninst, 100, 1000, 31)
+    probs, searches = [], []
+    for q, n in enumerate(sizes):
+        x, y = workloads.clustered_instance(int(n), 40_000 + q)
+        probs.append(mlpgpu.Problem.from_coords(x, y, dist_round=True))
+        for r in range(starts):
+            searches.append((q, workloads.random_perm_tour(int(n), 50_000 + starts * q + r)))
+    b = mlpgpu.Batch()
+    b.set_stream(stream.cuda_stream)
+    for q, t in searches:
+        b.add(probs[q], t)
+    b.run()  # warm-up (builds the job set)
+    b.reset()
+    torch.cuda.synchronize()
+    e0, e1 = _events(2)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    t0 = time.perf_counter()
+    b.run()
+    t1 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    torch.cuda.synchronize()
+    t_batch = e0.elapsed_time(e1) * 1e-3
+    res = [b.result(j)[1] for j in range(len(searches))]
+    evals = sum(r["evals"] for r in res)
+    # Plain form on every k-th search (the same searches, one instance per launch).
+    k = max(1, len(searches) // args.plain_sample)
+    sample = list(range(0, len(searches), k))
+    t_plain = 0.0
+    solvers = {}
+    for j in sample:
+        q, t = searches[j]
+        s = solvers.get(q)
+        if s is None:
+            s = solvers[q] = mlpgpu.Solver(probs[q])
+            s.set_stream(stream.cuda_stream)
+        s.set_tour(t)
+        torch.cuda.synchronize()
+        a, c = _events(2)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            st = s.dvnd()
+            c.record(stream)
+        torch.cuda.synchronize()
+        t_plain += a.elapsed_time(c) * 1e-3
+        assert st["cost"] == res[j]["cost"] and st["sweeps"] == res[j]["sweeps"], "batched and plain differ"
+    plain_solves = len(sample) / t_plain
+    batched_solves = len(searches) / t_batch
+    return {
+        "workload": f"{ninst} instances x {starts} starts = {len(searches)} DVND searches, n log-uniform "
+                    "[100,1000], 8-cluster coordinates (sigma 50), one batch",
+        "searches": len(searches), "seconds": t_batch, "host_seconds": t1 - t0,
+        "solves_per_s": batched_solves, "evals_per_s": evals / t_batch,
+        "sweeps_total": sum(r["sweeps"] for r in res),
+        "plain_solves_per_s": plain_solves, "plain_sample": len(sample),
+        "speedup_vs_plain": batched_solves / plain_solves,
+        "results_equal_plain": True,
+    }
+
+
+def bench_serving(args, mlpgpu, workloads):
+    """configs[4]: open-loop Poisson stream of requests, n log-uniform in
+    [50, 2000], half uniform / half 8-cluster coordinates, each a full DVND
+    from a seeded random start, admitted against a 40 GB device budget."""
+    nreq = args.serve_requests
+    sizes = workloads.log_uniform_sizes(nreq, 50, 2000, 77)
+    reqs = []
+    for k, n in enumerate(sizes):
+        n = int(n)
+        gen = workloads.uniform_instance if k % 2 == 0 else workloads.clustered_instance
+        x, y = gen(n, 70_000 + k)
+        reqs.append((x, y, workloads.random_perm_tour(n, 70_000 + k)))
+    out = {"workload": f"{nreq} requests, Poisson arrivals, n log-uniform [50,2000], half uniform / half "
+                       "8-cluster coordinates, full DVND each, admission budget 40 GB",
+           "budget_bytes": 40 << 30, "max_active": args.serve_slots, "iters_per_step": args.serve_iters,
+           "rates": []}
+    for rate in [float(r) for r in args.serve_rates.split(",")]:
+        srv = mlpgpu.Server(40 << 30, wide=False, max_active=args.serve_slots)
+        rng = np.random.default_rng(99)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        lat, done, i, rid_n = [], 0, 0, {}
+        first = last = None
+        base = srv.now()
+        steps = 0
+        while done < nreq:
+            now = srv.now() - base
+            while i < nreq and arrivals[i] <= now:
+                x, y, t = reqs[i]
+                rid_n[srv.submit(x, y, t, arrival=base + float(arrivals[i]))] = len(x)
+                i += 1
+            a, qd = srv.step(args.serve_iters)
+            steps += 1
+            if a == 0 and qd == 0 and i < nreq:
+                # idle: wait for the next arrival
+                while srv.now() - base < arrivals[i]:
+                    pass
+            for rid in srv.finished():
+                _, st, info = srv.result(rid, rid_n.pop(rid))
+                assert info["status"] == 0, info
+                lat.append(info["finished"] - info["arrival"])
+                first = info["arrival"] if first is None else min(first, info["arrival"])
+                last = info["finished"] if last is None else max(last, info["finished"])
+                done += 1
+        span = last - (base + float(arrivals[0]))
+        out["rates"].append({"offered_per_s": rate, "solves_per_s": nreq / span, "p50_s": _pct(lat, 0.50),
+                             "p99_s": _pct(lat, 0.99), "mean_s": statistics.mean(lat), "steps": steps})
+        srv.close()
+    # Plain per-request form on a sample: build the instance, solve alone.
+    import torch
+
+    k = max(1, nreq // args.plain_sample)
+    t_plain, cnt = 0.0, 0
+    for j in range(0, nreq, k):
+        x, y, t = reqs[j]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p = mlpgpu.Problem.from_coords(x, y, dist_round=True)
+        s = mlpgpu.Solver(p)
+        s.set_tour(t)
+        s.dvnd()
+        s.tour()
+        t_plain += time.perf_counter() - t0
+        cnt += 1
+        s.close()
+        p.close()
+    out["plain_solves_per_s"] = cnt / t_plain
+    out["plain_sample"] = cnt
+    return out
+
+
+def bench_large(args, mlpgpu, workloads, stream, flush):
+    """configs[3]: n = 10000, int64 costs, D (400 MB) in HBM: one Or-opt-3 +
+    2-opt sweep against the HBM roofline, and a DVND capped in sweeps."""
+    import torch
+
+    n = args.large_n
+    size = n + 1
+    x, y = workloads.uniform_instance(n, INSTANCE_SEED + 1)
+    prob = mlpgpu.Problem.from_coords(x, y, dist_round=True)
+    s = mlpgpu.Solver(prob, wide=True)
+    s.set_stream(stream.cuda_stream)
+    s.set_tour(workloads.random_perm_tour(n, 5))
+    mask = (1 << mlpgpu.NB_2OPT) | (1 << mlpgpu.NB_OROPT3)
+    t_sw = time_sweep(mlpgpu, s, stream, flush, mask, 5)
+    ev = sum(blocks(nb, size) * threads(nb, size) for nb in (1, 4))
+    byts = sum(blocks(nb, size) * threads(nb, size) * BYTES_PER_EVAL[nb] for nb in (1, 4))
+    s.set_tour(workloads.random_perm_tour(n, 5))
+    torch.cuda.synchronize()
+    a, c = _events(2)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        st = s.dvnd(mlpgpu.NB_ALL, args.large_iters)
+        c.record(stream)
+    torch.cuda.synchronize()
+    t_d = a.elapsed_time(c) * 1e-3
+    return {"workload": f"n={n} uniform, int64 costs, 2-opt + Or-opt-3 sweep; DVND capped at "
+                        f"{args.large_iters} sweeps", "n": n,
+            "sweep_2opt_oropt3": {"evals": ev, "us": t_sw * 1e6, "evals_per_s": ev / t_sw,
+                                  "algorithmic_bytes": byts, "achieved_gbs": byts / t_sw / 1e9},
+            "dvnd_capped": {"sweeps": st["sweeps"], "moves": st["moves"], "seconds": t_d,
+                            "evals_per_s": st["evals"] / t_d, "cost": st["cost"], "converged": st["converged"]}}
+
+
 def run_ours(args, world, rank, local) -> None:
     import torch
 
@@ -249,141 +541,71 @@ def run_ours(args, world, rank, local) -> None:
     import mlpgpu
     from mlpgpu import workloads
 
-    lib = mlpgpu.lib()
-    _ = lib
     mlpgpu._check(mlpgpu.lib().mlp_set_device(local))
-    n = N_NODES
-    size = n + 1
-    x, y = workloads.uniform_instance(n, INSTANCE_SEED)
-    prob = mlpgpu.Problem.from_coords(x, y, dist_round=True)
-    solver = mlpgpu.Solver(prob, wide=False)
     stream = torch.cuda.Stream()
-    solver.set_stream(stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")  # > 129 MB L2
+    wl = set(args.workloads.split(","))
+    if args.only:
+        # One workload alone (profiling runs); prints its object, not the bench line.
+        fn = {"batched": lambda: bench_batched(args, mlpgpu, workloads, stream),
+              "serving": lambda: bench_serving(args, mlpgpu, workloads),
+              "large": lambda: bench_large(args, mlpgpu, workloads, stream, flush)}[args.only]
+        if rank == 0:
+            print(json.dumps({args.only: fn()}))
+        return
 
-    # Start tours (a distinct seeded start per step and rank) staged in HBM.
-    nsteps = args.warmup + args.steps
-    tours = [workloads.random_perm_tour(n, 1_000 * rank + k) for k in range(nsteps)]
-    tours_dev = torch.tensor(np.stack(tours), dtype=torch.int32, device="cuda")
-    solver.set_tour(tours[0])
-    shape = solver.autotune() if args.autotune else None
-
-    # ---- sweep kernel timing (roofline) ----
-    ev = sweep_evals(size)
-    sb = sweep_bytes(size)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.sweeps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.sweeps)]
-    with torch.cuda.stream(stream):
-        for _ in range(3):
-            solver.sweep(mlpgpu.NB_ALL, 1)
-        for r in range(args.sweeps):
-            flush.zero_()
-            starts[r].record(stream)
-            solver.sweep(mlpgpu.NB_ALL, 1)
-            ends[r].record(stream)
-    torch.cuda.synchronize()
-    # mlp_solver_sweep also enqueues a prepare (key reset) after the sweep kernel;
-    # time a prepare alone and subtract it to isolate the sweep kernel.
-    pst = [torch.cuda.Event(enable_timing=True) for _ in range(args.sweeps)]
-    pen = [torch.cuda.Event(enable_timing=True) for _ in range(args.sweeps)]
-    with torch.cuda.stream(stream):
-        for r in range(args.sweeps):
-            flush.zero_()
-            pst[r].record(stream)
-            solver.sweep(mlpgpu.NB_ALL, 0)
-            pen[r].record(stream)
-    torch.cuda.synchronize()
-    t_sweep_prep = statistics.median(s.elapsed_time(e) for s, e in zip(starts, ends)) * 1e-3
-    t_prep = statistics.median(s.elapsed_time(e) for s, e in zip(pst, pen)) * 1e-3
-    t_sweep = max(t_sweep_prep - t_prep, 1e-9)
-
-    # ---- DVND steps: device time, tours resident in HBM ----
-    step_ms, step_evals, step_sweeps, costs = [], [], [], []
-    sampler = ClockSampler(local)
-    for k in range(nsteps):
-        if k == args.warmup:
-            sampler.start()
-            if world > 1:
-                torch.distributed.barrier()
-            torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0.record(stream)
-            solver.set_tour_device(tours_dev[k].data_ptr())
-            solver.dvnd_async(mlpgpu.NB_ALL)
-            e1.record(stream)
-        torch.cuda.synchronize()
-        st = solver.stats()
-        if k >= args.warmup:
-            step_ms.append(e0.elapsed_time(e1))
-            step_evals.append(st["evals"])
-            step_sweeps.append(st["sweeps"])
-            costs.append(st["cost"])
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-
-    # ---- e2e through the C-ABI with host buffers ----
-    host_tours = [torch.from_numpy(t).pin_memory() for t in tours]
-    out = torch.empty(size, dtype=torch.int32).pin_memory()
-    e2e_s, e2e_evals = [], []
-    for k in range(nsteps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        mlpgpu._check(mlpgpu.lib().mlp_solver_set_tour(solver._h, mlpgpu.C.c_void_p(host_tours[k].data_ptr()), size))
-        st = mlpgpu.DvndStats()
-        mlpgpu._check(mlpgpu.lib().mlp_solver_dvnd(solver._h, mlpgpu.NB_ALL, 1 << 20, mlpgpu.C.byref(st)))
-        mlpgpu._check(mlpgpu.lib().mlp_solver_get_tour(solver._h, mlpgpu.C.c_void_p(out.data_ptr()), size))
-        dt = time.perf_counter() - t0
-        if k >= args.warmup:
-            e2e_s.append(dt)
-            e2e_evals.append(st.evals)
-            assert st.cost == costs[k - args.warmup], "e2e and device runs disagree"
-
-    total_s = sum(step_ms) * 1e-3
-    agg = reduce_sum([float(sum(step_evals)), float(len(step_ms)), float(sum(e2e_evals))], world)
-    tmax = reduce_max([total_s, sum(e2e_s)], world)
+    P = bench_plain(args, world, rank, mlpgpu, workloads, stream, flush)
+    size = P["size"]
+    total_s = sum(P["step_ms"]) * 1e-3
+    agg = reduce_sum([float(sum(P["step_evals"])), float(len(P["step_ms"])), float(sum(P["e2e_evals"]))], world)
+    tmax = reduce_max([total_s, sum(P["e2e_s"])], world)
     value = agg[0] / tmax[0]
     solves = agg[1] / tmax[0]
     e2e_value = agg[2] / tmax[1]
+    extra = {}
+    if rank == 0:
+        if "batched" in wl:
+            extra["batched"] = bench_batched(args, mlpgpu, workloads, stream)
+        if "serving" in wl:
+            extra["serving"] = bench_serving(args, mlpgpu, workloads)
+        if "large" in wl:
+            extra["large"] = bench_large(args, mlpgpu, workloads, stream, flush)
     if rank != 0:
         return
-    lat = sorted(step_ms)
-    p = lambda q: lat[min(len(lat) - 1, max(0, math.ceil(q * len(lat)) - 1))]
     peaks = measured_peaks()
-    achieved = sb / t_sweep / 1e9
-    launches = 0
-    for s in step_sweeps:
-        body = (s + 1) // 2
-        launches += 2 + 5 * body  # prepare + stats, then per loop body: 2 x (sweep + merge) + condition
+    sb = sweep_bytes(size)
+    ev = sweep_evals(size)
+    achieved = sb / P["t_sweep"] / 1e9
+    launches = sum(plain_launches(s) for s in P["step_sweeps"])
     traffic = ncu_traffic_per_sweep()
+    step_ms = P["step_ms"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded uniform coordinates in [0,1000]^2, EUC_2D nint int32 distances)",
         "config": {"workload": "plain DVND n=1000 to local optimum (swap, 2-opt, Or-opt-1/2/3), one instance "
-                               "per launch, seeded random start per step",
-                   "n": n, "evals_per_sweep": ev, "l2": "flushed (256 MB write) before every timed step",
-                   "tile_shape": shape, "replicas": world},
+                               "per launch sequence, seeded random start per step",
+                   "n": P["n"], "evals_per_sweep": ev, "l2": "flushed (256 MB write) before every timed step",
+                   "tile_shape": P["shape"], "replicas": world,
+                   "loop": "host-checked replays of 16-iteration CUDA graphs"},
         "dvnd_solves_per_s": solves,
-        "latency_ms": {"p50": p(0.50), "p99": p(0.99), "mean": statistics.mean(step_ms)},
-        "sweeps_per_solve": statistics.mean(step_sweeps),
-        "sweep": {"evals": ev, "us": t_sweep * 1e6, "evals_per_s": ev / t_sweep},
+        "latency_ms": {"p50": _pct(step_ms, 0.50), "p99": _pct(step_ms, 0.99), "mean": statistics.mean(step_ms)},
+        "sweeps_per_solve": statistics.mean(P["step_sweeps"]),
+        "us_per_iteration": 1e3 * sum(step_ms) / sum(P["step_sweeps"]),
+        "sweep": {"evals": ev, "us": P["t_sweep"] * 1e6, "evals_per_s": ev / P["t_sweep"]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": size * 4,
                 "d2h_bytes_per_step": size * 4 + 16 * 8},
-        "roofline": {"kernel": "k_sweep (all five neighbourhoods)", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "k_sweep (all five neighbourhoods, n=1000)", "bound": "hbm", "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                      "traffic": traffic, "algorithmic_bytes_per_launch": sb,
                      "peak_source": peaks["source"] + " hbm_gbs (STREAM copy)"},
-        "clocks": clocks,
+        "clocks": P["clocks"],
         "gpu_launches": launches,
     }
+    line.update(extra)
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(n, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = cpu_baseline(P["n"], budget_s=args.cpu_budget)
     print(json.dumps(line))
 
 
@@ -398,6 +620,18 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-iters", type=int, default=1 << 20)
+    ap.add_argument("--workloads", default="batched,serving,large",
+                    help="extra workloads reported beside the plain n=1000 headline")
+    ap.add_argument("--batch-instances", type=int, default=512)
+    ap.add_argument("--plain-sample", type=int, default=128)
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-rates", default="250,500,1000")
+    ap.add_argument("--serve-slots", type=int, default=1024)
+    ap.add_argument("--serve-iters", type=int, default=2)
+    ap.add_argument("--large-n", type=int, default=10000)
+    ap.add_argument("--large-iters", type=int, default=300)
+    ap.add_argument("--only", choices=["batched", "serving", "large"], default=None,
+                    help="run one extra workload alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

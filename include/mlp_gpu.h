@@ -109,10 +109,11 @@ MLP_API void mlp_solver_destroy(mlp_solver_t s);
 /* Stream on which every later call of this solver runs (NULL: the solver's own). */
 MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
 /* Sweep tile shape index (0..7: diagonals x rows = 32x4, 32x8, 32x16, 64x4, 64x8,
- * 64x16, 128x8, 128x16).  Loop mode: iterations = 0 (default) runs the
- * DVND loop on the device (a CUDA-graph while node, no host round trips);
- * iterations >= 1 replays graphs of that many iterations and checks convergence
- * on the host in between. */
+ * 64x16, 128x8, 128x16).  Loop mode of mlp_solver_dvnd: iterations >= 1
+ * (default 16) replays CUDA graphs of that many iterations and checks
+ * convergence on the host in between; iterations = 0 runs the whole loop on
+ * the device (a CUDA-graph while node, no host round trips; always the mode
+ * of mlp_solver_dvnd_async). */
 MLP_API int mlp_solver_set_tile_shape(mlp_solver_t s, int32_t shape);
 MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t iterations);
 /* Tour of `len` = size entries: tour[0] = tour[size-1] = 0 and a permutation of

@@ -225,3 +225,25 @@ def test_large_sizes_use_global_merge_workspace(mlpgpu_mod):
     b.run(max_iters=6)
     assert np.array_equal(b.result(0)[0], oracle.dvnd(ts, Ds, max_iters=6)[0])
     assert np.array_equal(b.result(1)[0], ot)
+
+
+def test_large_n10000_wide_candidates_and_capped_dvnd(mlpgpu_mod):
+    """n = 10000 with int64 costs (400 MB distance matrix in HBM): cost,
+    2-opt and Or-opt-3 candidates and a DVND capped at two sweeps, all equal
+    to the oracle's."""
+    import os
+
+    n = 10000
+    x, y = oracle.uniform_instance(n, 2025)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, 5)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True), wide=True)
+    s.set_tour(t)
+    assert s.cost() == oracle.cost(t, D, True)
+    for nb in (1, 4):
+        c, i, j = s.eval(nb)
+        oc, oi, oj, _ = oracle.eval_nb(nb, t, D, True)
+        assert np.array_equal(c, oc) and np.array_equal(i, oi) and np.array_equal(j, oj), nb
+    st = s.dvnd(mlpgpu_mod.NB_ALL, 2)
+    ot, ost = oracle.dvnd(t, D, wide=True, max_iters=2, threads=os.cpu_count() or 1)
+    assert np.array_equal(s.tour(), ot) and st["cost"] == ost["cost"] and st["moves"] == ost["moves"]

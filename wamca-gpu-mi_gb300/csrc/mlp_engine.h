@@ -153,7 +153,7 @@ class JobSet {
   cudaStream_t stream_;
   int shape_ = -1;
   int unroll_ = 16;
-  bool device_loop_ = true;
+  bool device_loop_ = false;
   int mask_ = 0x1f;
   int max_size_ = 0;
   bool merge_smem_ = true;

@@ -334,10 +334,13 @@ void job_tiles(int size, int shape, std::vector<SweepTile>* out) {
     for (int L0 = 1; r0 + L0 <= size - 2; L0 += ts.tl) out->push_back(SweepTile{0, r0, L0, 0});
 }
 
-int default_shape(int size) {
-  if (size <= 400) return 0;    // 32 diagonals x 4 rows
-  if (size <= 2000) return 1;   // 32 x 8
-  return 7;                     // 128 x 16
+int default_shape(int size, int njobs) {
+  // Measured on GB300: one n=1000 job is latency-bound and prefers many small
+  // tiles; a set of many jobs is throughput-bound and prefers 64 x 8.
+  if (size > 2000) return 7;    // 128 diagonals x 16 rows
+  if (njobs >= 8) return 4;     // 64 x 8
+  if (size <= 400) return 0;    // 32 x 4
+  return 3;                     // 64 x 4
 }
 
 // ---------------------------------------------------------------- JobSet
@@ -391,7 +394,7 @@ int JobSet::init() {
   MLP_CUDA(cudaMemcpyAsync(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice, stream_),
            "copy jobs");
   MLP_CUDA(cudaStreamSynchronize(stream_), "copy jobs");
-  if (shape_ < 0) shape_ = default_shape(max_size_);
+  if (shape_ < 0) shape_ = default_shape(max_size_, (int)jobs_.size());
   return build_tiles();
 }
 
@@ -519,7 +522,7 @@ int JobSet::prepare(bool reset_stats) {
 }
 
 int JobSet::launch_iteration() {
-  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
+  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
   MLP_CUDA(launch_merge(djobs_, (int)jobs_.size(), wide_, merge_smem_, max_size_, stream_), "merge kernel");
   return kOk;
 }
@@ -530,12 +533,12 @@ int JobSet::sweep_only() {
     if (st != kOk) return st;
   }
   MLP_CUDA(launch_stats_begin(djobs_, (int)jobs_.size(), 1, stream_), "stats kernel");
-  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
+  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, false, stream_), "sweep kernel");
   return kOk;
 }
 
 int JobSet::sweep_kernel() {
-  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
+  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, false, stream_), "sweep kernel");
   return kOk;
 }
 

@@ -168,6 +168,7 @@ class JobSet {
   int loop_unroll_ = 0;
 };
 
-int default_shape(int size);
+// Sweep tile shape for a job set whose largest tour has `size` positions.
+int default_shape(int size, int njobs);
 
 }  // namespace mlp

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(1024) k_prepare(const JobDev* __restrict__ job
 // --------------------------------------------------------------------------
 template <bool WIDE, int TL, int TR>
 __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tiles,
-                                              const JobDev* __restrict__ jobs) {
+                                              const JobDev* __restrict__ jobs, int improve_only) {
   using Ar = Arith<WIDE>;
   using C = typename Ar::C;
   using V = typename Ar::V;
@@ -238,7 +238,6 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   const SweepTile tile = tiles[blockIdx.x];
   const JobDev* J = jobs + tile.job;
   const int64_t* stats = J->stats;
-  if (stats[kStatConverged] || stats[kStatSweeps] >= stats[kStatLimit]) return;
   const int sz = J->size, n = J->n, mask = J->nb_mask;
   const int r0 = tile.r0, L0 = tile.L0, tid = threadIdx.x;
   const int pad = sz + 8;
@@ -248,6 +247,9 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   const int32_t* __restrict__ Ag = J->A;
   const C* __restrict__ W = (const C*)J->W;
   const C* __restrict__ Q = (const C*)J->Q;
+  // Loaded with the tile's other independent loads; a job that converged or
+  // used its sweep limit is skipped after the staging barriers.
+  const bool done = stats[kStatConverged] || stats[kStatSweeps] >= stats[kStatLimit];
 
   for (int q = tid; q < SR; q += TL) {
     const int p = r0 - 1 + q;
@@ -302,6 +304,7 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
     }
   }
   __syncthreads();
+  if (done) return;
 
   uint64_t* keys = J->keys;
   const int L = L0 + tid, b = tid + 1, lane = tid & 31;
@@ -313,7 +316,12 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   const bool has2B = blk2B >= 0 && blk2B < nb2;
   V b2A = kInf, b2B = kInf, bF[3] = {kInf, kInf, kInf}, bB[3] = {kInf, kInf, kInf};
   int c2A = -1, c2B = -1, cF[3] = {-1, -1, -1}, cB[3] = {-1, -1, -1};
-
+  // E(x, y) around the pair (r, c) of row a; the four that row a + 1 shares
+  // with row a are carried in registers.
+  C sM1P1 = (C)sS[0][b + 1];  // E(r-1, c)
+  C s0M1 = (C)sS[1][b - 1];   // E(r, c-1)
+  C s0P1 = (C)sS[1][b + 1];   // E(r, c+1)
+  C sP1P1 = (C)sS[2][b + 1];  // E(r+1, c+2)
 #pragma unroll 1
   for (int a = 1; a <= TR; a++) {
     const int r = r0 + a - 1;
@@ -321,14 +329,10 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
     const int c = r + L;
     const bool vpair = c <= sz - 2;
     const int qr = a - 1, qc = a + tid;
-    const C sM1P1 = (C)sS[a - 1][b + 1];
-    const C s0M1 = (C)sS[a][b - 1];
-    const C s00 = (C)sS[a][b];
-    const C s0P1 = (C)sS[a][b + 1];
-    const C s0P2 = (C)sS[a][b + 2];
-    const C sP1M1 = (C)sS[a + 1][b - 1];
-    const C sP1P1 = (C)sS[a + 1][b + 1];
-    const C sP2P1 = (C)sS[a + 2][b + 1];
+    const C sP1M1 = (C)sS[a + 1][b - 1];  // E(r+1, c)
+    const C s00 = (C)sS[a][b];            // E(r, c)
+    const C s0P2 = (C)sS[a][b + 2];       // E(r, c+2)
+    const C sP2P1 = (C)sS[a + 2][b + 1];  // E(r+2, c+3)
     const C wr0 = (C)sRw[qr], wr1 = (C)sRw[qr + 1];
     const C wc0 = (C)sCw[qc], wc1 = (C)sCw[qc + 1];
     const C Wr0 = sRW[qr], Wc0 = sCW[qc];
@@ -346,14 +350,15 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
       if (!WIDE) {
         const uint32_t u = (v && d != kInf) ? ((uint32_t)d ^ 0x80000000u) : 0xffffffffu;
         const uint32_t mn = __reduce_min_sync(kFull, u);
-        any = mn != 0xffffffffu;
+        any = improve_only ? mn < 0x80000000u : mn != 0xffffffffu;
         ties = __ballot_sync(kFull, u == mn);
       } else {
         const uint64_t u = v ? (uint64_t)((int64_t)d + (int64_t)kCostBias) : ~0ull;
         const uint32_t hi = (uint32_t)(u >> 32), lo = (uint32_t)u;
         const uint32_t mh = __reduce_min_sync(kFull, hi);
         const uint32_t ml = __reduce_min_sync(kFull, hi == mh ? lo : 0xffffffffu);
-        any = !(mh == 0xffffffffu && ml == 0xffffffffu);
+        const uint64_t mn = ((uint64_t)mh << 32) | ml;
+        any = improve_only ? mn < kCostBias : mn != ~0ull;
         ties = __ballot_sync(kFull, hi == mh && lo == ml);
       }
       if (any) {
@@ -406,21 +411,28 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
         }
       }
     }
+    sM1P1 = s0P1;
+    s0M1 = sP1M1;
+    s0P1 = sP1P1;
+    sP1P1 = sP2P1;
   }
 
-  if (c2A >= 0)
+  // DVND sweeps publish improving candidates only (the merge ignores the
+  // rest); evaluation sweeps publish every block's best.
+
+  if (c2A >= 0 && (!improve_only || b2A < 0))
     atomicMin((unsigned long long*)&keys[off1 + (L - 1)],
               (unsigned long long)make_key((int64_t)b2A, (uint32_t)(c2A - 2), kCtxBits));
-  if (c2B >= 0)
+  if (c2B >= 0 && (!improve_only || b2B < 0))
     atomicMin((unsigned long long*)&keys[off1 + blk2B],
               (unsigned long long)make_key((int64_t)b2B, (uint32_t)(sz - 2 - c2B), kCtxBits));
 #pragma unroll
   for (int k = 1; k <= 3; k++) {
     const int offk = nb_offset(k + 1, sz);
-    if (cF[k - 1] >= 0)
+    if (cF[k - 1] >= 0 && (!improve_only || bF[k - 1] < 0))
       atomicMin((unsigned long long*)&keys[offk + (L - 1)],
                 (unsigned long long)make_key((int64_t)bF[k - 1], (uint32_t)(cF[k - 1] - 2), kCtxBits));
-    if (cB[k - 1] >= 0)
+    if (cB[k - 1] >= 0 && (!improve_only || bB[k - 1] < 0))
       atomicMin((unsigned long long*)&keys[offk + (sz - k - 1 - L)],
                 (unsigned long long)make_key((int64_t)bB[k - 1], (uint32_t)(sz - k - 1 - cB[k - 1]),
                                              kCtxBits));
@@ -1094,23 +1106,24 @@ __global__ void k_loop_condition(const JobDev* __restrict__ jobs, int njobs, cud
 }
 
 template <bool WIDE, int TL, int TR>
-cudaError_t sweep_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, cudaStream_t s) {
-  k_sweep<WIDE, TL, TR><<<ntiles, TL, 0, s>>>(tiles, jobs);
+cudaError_t sweep_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, int improve_only,
+                         cudaStream_t s) {
+  k_sweep<WIDE, TL, TR><<<ntiles, TL, 0, s>>>(tiles, jobs, improve_only);
   return cudaGetLastError();
 }
 
 template <bool WIDE>
-cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape,
+cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape, int improve_only,
                            cudaStream_t s) {
   switch (shape) {
-    case 0: return sweep_launch<WIDE, 32, 4>(tiles, ntiles, jobs, s);
-    case 1: return sweep_launch<WIDE, 32, 8>(tiles, ntiles, jobs, s);
-    case 2: return sweep_launch<WIDE, 32, 16>(tiles, ntiles, jobs, s);
-    case 3: return sweep_launch<WIDE, 64, 4>(tiles, ntiles, jobs, s);
-    case 4: return sweep_launch<WIDE, 64, 8>(tiles, ntiles, jobs, s);
-    case 5: return sweep_launch<WIDE, 64, 16>(tiles, ntiles, jobs, s);
-    case 6: return sweep_launch<WIDE, 128, 8>(tiles, ntiles, jobs, s);
-    case 7: return sweep_launch<WIDE, 128, 16>(tiles, ntiles, jobs, s);
+    case 0: return sweep_launch<WIDE, 32, 4>(tiles, ntiles, jobs, improve_only, s);
+    case 1: return sweep_launch<WIDE, 32, 8>(tiles, ntiles, jobs, improve_only, s);
+    case 2: return sweep_launch<WIDE, 32, 16>(tiles, ntiles, jobs, improve_only, s);
+    case 3: return sweep_launch<WIDE, 64, 4>(tiles, ntiles, jobs, improve_only, s);
+    case 4: return sweep_launch<WIDE, 64, 8>(tiles, ntiles, jobs, improve_only, s);
+    case 5: return sweep_launch<WIDE, 64, 16>(tiles, ntiles, jobs, improve_only, s);
+    case 6: return sweep_launch<WIDE, 128, 8>(tiles, ntiles, jobs, improve_only, s);
+    case 7: return sweep_launch<WIDE, 128, 16>(tiles, ntiles, jobs, improve_only, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -1141,10 +1154,11 @@ cudaError_t launch_prepare(const JobDev* jobs, int njobs, bool wide, bool reset_
 }
 
 cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
-                         int shape, cudaStream_t s) {
+                         int shape, bool improve_only, cudaStream_t s) {
   if (ntiles <= 0) return cudaSuccess;
-  return wide ? sweep_dispatch<true>(tiles, ntiles, jobs, shape, s)
-              : sweep_dispatch<false>(tiles, ntiles, jobs, shape, s);
+  const int io = improve_only ? 1 : 0;
+  return wide ? sweep_dispatch<true>(tiles, ntiles, jobs, shape, io, s)
+              : sweep_dispatch<false>(tiles, ntiles, jobs, shape, io, s);
 }
 
 cudaError_t configure_prepare() {

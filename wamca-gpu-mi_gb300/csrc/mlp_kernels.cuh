@@ -37,8 +37,10 @@ cudaError_t configure_prepare();
 cudaError_t launch_stats_begin(const JobDev* jobs, int njobs, int64_t limit, cudaStream_t s);
 cudaError_t launch_prepare(const JobDev* jobs, int njobs, bool wide, bool reset_stats,
                            cudaStream_t s);
+// improve_only: publish only improving candidates (DVND iterations; the
+// merge ignores the others); false publishes every block's best (evaluation).
 cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
-                         int shape, cudaStream_t s);
+                         int shape, bool improve_only, cudaStream_t s);
 cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
                          cudaStream_t s);
 // Reference ADS buffer (source/mlads.h:38-74) of each job's current tour.

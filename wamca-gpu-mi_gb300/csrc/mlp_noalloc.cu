@@ -194,7 +194,7 @@ extern "C" MLP_API int mlp_eval_noalloc(const int32_t* dist_dev, int32_t n, cons
   int ntiles = 0;
   for (int r0 = 1; r0 <= size - 3; r0 += kNaTR) ntiles += (size - 2 - r0 + kNaTL - 1) / kNaTL;
   st = cuda_status(launch_sweep(reinterpret_cast<const SweepTile*>(base + lay.tiles), ntiles, job, wide != 0,
-                                kNoAllocShape, s),
+                                kNoAllocShape, false, s),
                    "sweep kernel");
   if (st != kOk) return st;
   const int m = nb_blocks(nb, size);

@@ -292,7 +292,7 @@ static int server_step(mlp_server* s, int iters) {
         max_large = std::max(max_large, sz);
       }
     }
-    const int shape = s->shape >= 0 ? s->shape : default_shape(max_size);
+    const int shape = s->shape >= 0 ? s->shape : default_shape(max_size, nact);
     size_t ntiles = 0;
     for (int q = 0; q < nact; q++) {
       const int sz = s->active[q].job->size;
@@ -314,7 +314,7 @@ static int server_step(mlp_server* s, int iters) {
     MLP_CUDA(cudaMemcpyAsync(s->dtiles, s->htiles, sizeof(SweepTile) * t, cudaMemcpyHostToDevice, s->stream),
              "copy tiles");
     for (int it = 0; it < iters; it++) {
-      MLP_CUDA(launch_sweep(s->dtiles, (int)t, s->djobs, s->wide, shape, s->stream), "sweep kernel");
+      MLP_CUDA(launch_sweep(s->dtiles, (int)t, s->djobs, s->wide, shape, true, s->stream), "sweep kernel");
       MLP_CUDA(launch_merge(s->djobs, ksmall, s->wide, true, max_small, s->stream), "merge kernel");
       MLP_CUDA(launch_merge(s->djobs + ksmall, nact - ksmall, s->wide, false, max_large, s->stream),
                "merge kernel");

@@ -198,6 +198,10 @@ MLP_API int mlp_batch_reset(mlp_batch_t b);
 MLP_API int mlp_batch_result(mlp_batch_t b, int32_t job, int32_t* tour, int32_t len,
                              mlp_dvnd_stats_t* stats);
 MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape);
+/* Merge kernel of the batch's iterations: 0 = automatic (one CTA per job for
+ * 16 jobs or more, otherwise a six-CTA cluster per job), 1 = cluster, 2 = one
+ * CTA per job.  Every mode gives the same results. */
+MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode);
 
 /* ---- serving form: continuous batching of arriving searches ----
  * A server owns a CUDA stream and a device memory pool.  Requests (instance

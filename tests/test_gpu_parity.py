@@ -247,3 +247,38 @@ def test_large_n10000_wide_candidates_and_capped_dvnd(mlpgpu_mod):
     st = s.dvnd(mlpgpu_mod.NB_ALL, 2)
     ot, ost = oracle.dvnd(t, D, wide=True, max_iters=2, threads=os.cpu_count() or 1)
     assert np.array_equal(s.tour(), ot) and st["cost"] == ost["cost"] and st["moves"] == ost["moves"]
+
+
+def test_batch_merge_kernels_give_identical_results(mlpgpu_mod):
+    """The one-CTA-per-job merge (large batches) and the six-CTA cluster merge
+    select and apply the same moves: 20 jobs of mixed sizes, including one
+    whose one-CTA merge runs from a global workspace (n = 3200), agree with
+    each other, with the plain solver and with the oracle."""
+    sizes = [30, 45, 60, 77, 90, 101, 120, 150, 180, 200, 230, 260, 300, 350, 400, 480, 560, 700, 1200, 3200]
+    cases = []
+    for q, n in enumerate(sizes):
+        x, y = (oracle.clustered_instance if q % 2 else oracle.uniform_instance)(n, 900 + q)
+        cases.append((mlpgpu_mod.Problem.from_coords(x, y, dist_round=True), x, y, oracle.random_perm_tour(n, 900 + q)))
+    limit = 12
+    out = {}
+    for mode in (1, 2, 0):
+        b = mlpgpu_mod.Batch()
+        b.set_merge_mode(mode)
+        for p, _, _, t in cases:
+            b.add(p, t)
+        b.run(max_iters=limit)
+        out[mode] = [b.result(j) for j in range(len(cases))]
+    for j in range(len(cases)):
+        (t1, s1), (t2, s2), (t0, s0) = out[1][j], out[2][j], out[0][j]
+        assert np.array_equal(t1, t2) and s1 == s2, j
+        assert np.array_equal(t0, t1) and s0 == s1, j
+    for j in (0, 5, 11, 19):
+        p, x, y, t = cases[j]
+        s = mlpgpu_mod.Solver(p)
+        s.set_tour(t)
+        st = s.dvnd(max_iters=limit)
+        assert np.array_equal(s.tour(), out[2][j][0]) and st == out[2][j][1], j
+    for j in (0, 3, 9):
+        p, x, y, t = cases[j]
+        ot, ost = oracle.dvnd(t, oracle.dist(x, y, True), max_iters=limit)
+        assert np.array_equal(out[2][j][0], ot) and out[2][j][1]["cost"] == ost["cost"], j

@@ -496,6 +496,14 @@ MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape) {
   return kOk;
 }
 
+MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode) {
+  if (!b) return arg_error("null batch");
+  if (mode < kMergeAuto || mode > kMergeSolo) return arg_error("merge mode must be 0, 1 or 2");
+  b->merge_mode = mode;
+  if (b->set) return b->set->set_merge_mode(mode);
+  return kOk;
+}
+
 MLP_API int mlp_batch_add(mlp_batch_t b, mlp_problem_t h, const int32_t* tour, int32_t len, int32_t* job) {
   Problem* p = reinterpret_cast<Problem*>(h);
   if (!b || !p) return arg_error("null argument");
@@ -524,6 +532,7 @@ static int batch_build(mlp_batch* b) {
   for (auto& j : b->jobs) js.push_back(j.get());
   b->set.reset(new JobSet(js, b->wide, b->stream));
   if (b->shape >= 0) MLP_TRY(b->set->set_shape(b->shape));
+  MLP_TRY(b->set->set_merge_mode(b->merge_mode));
   MLP_TRY(b->set->init());
   return batch_upload(b);
 }

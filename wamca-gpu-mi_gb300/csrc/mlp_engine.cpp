@@ -259,7 +259,7 @@ size_t job_bytes(int size, bool wide, int moves_cap) {
   b += al(4 * 8);                       // kept_count
   b += al(8 * kStatWords);              // stats
   b += al(4 * (size_t)moves_cap) + al(8 * (size_t)moves_cap);
-  if (size > merge_smem_max_size()) b += al(merge_ws_bytes(size));
+  if (merge_needs_ws(size)) b += al(merge_ws_bytes(size));
   return b;
 }
 
@@ -316,7 +316,7 @@ static void job_layout(Job* j, Problem* p, bool wide, int moves_cap) {
   d.moves_out = moves_cap > 0 ? (uint32_t*)c : nullptr;  c += al(4 * (size_t)moves_cap);
   d.moves_cost = moves_cap > 0 ? (int64_t*)c : nullptr;  c += al(8 * (size_t)moves_cap);
   d.ws = nullptr;
-  if (size > merge_smem_max_size()) {
+  if (merge_needs_ws(size)) {
     d.ws = (uint8_t*)c;
     c += al(merge_ws_bytes(size));
   }
@@ -371,7 +371,8 @@ int JobSet::init() {
     max_size_ = std::max(max_size_, j->size);
   }
   merge_smem_ = max_size_ <= merge_smem_max_size();
-  if (!merge_smem_) {
+  solo_smem_ = max_size_ <= solo_smem_max_size();
+  if (!merge_smem_ || !solo_smem_) {
     // The merge runs from global workspaces: give one to every job lacking it.
     for (Job* j : jobs_) {
       if (j->dev.ws != nullptr) continue;
@@ -521,9 +522,30 @@ int JobSet::prepare(bool reset_stats) {
   return kOk;
 }
 
+bool JobSet::solo_merge() const {
+  return merge_mode_ == kMergeSolo || (merge_mode_ == kMergeAuto && (int)jobs_.size() >= kSoloMinJobs);
+}
+
 int JobSet::launch_iteration() {
   MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
-  MLP_CUDA(launch_merge(djobs_, (int)jobs_.size(), wide_, merge_smem_, max_size_, stream_), "merge kernel");
+  if (solo_merge())
+    MLP_CUDA(launch_merge_solo(djobs_, (int)jobs_.size(), wide_, solo_smem_, max_size_, stream_), "merge kernel");
+  else
+    MLP_CUDA(launch_merge(djobs_, (int)jobs_.size(), wide_, merge_smem_, max_size_, stream_), "merge kernel");
+  return kOk;
+}
+
+int JobSet::set_merge_mode(int mode) {
+  if (mode < kMergeAuto || mode > kMergeSolo) {
+    set_error("merge mode must be 0 (auto), 1 (cluster) or 2 (one CTA per job)");
+    return kErrArg;
+  }
+  if (mode == merge_mode_) return kOk;
+  merge_mode_ = mode;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+  if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
+  loop_graph_ = nullptr;
   return kOk;
 }
 

@@ -90,6 +90,9 @@ int job_create_async(Problem* p, bool wide, cudaMemPool_t pool, cudaStream_t str
 void job_tiles(int size, int shape, std::vector<SweepTile>* out);
 size_t job_bytes(int size, bool wide, int moves_cap);
 
+enum MergeMode : int { kMergeAuto = 0, kMergeCluster = 1, kMergeSolo = 2 };
+constexpr int kSoloMinJobs = 16;
+
 struct DvndResult {
   int64_t cost = 0;
   int64_t iterations = 0;   // iterations that applied moves
@@ -143,6 +146,10 @@ class JobSet {
   int ntiles() const { return ntiles_; }
   // One DVND iteration over the current jobs (no statistics reset).
   int launch_iteration();
+  // Merge kernel: kMergeAuto (one CTA per job for sets of kSoloMinJobs jobs
+  // or more, a six-CTA cluster per job otherwise), kMergeCluster, kMergeSolo.
+  int set_merge_mode(int mode);
+  bool solo_merge() const;
 
  private:
   int build_tiles();
@@ -157,6 +164,8 @@ class JobSet {
   int mask_ = 0x1f;
   int max_size_ = 0;
   bool merge_smem_ = true;
+  bool solo_smem_ = true;
+  int merge_mode_ = 0;
   JobDev* djobs_ = nullptr;
   SweepTile* dtiles_ = nullptr;
   int ntiles_ = 0;

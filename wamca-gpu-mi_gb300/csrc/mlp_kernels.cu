@@ -647,7 +647,204 @@ __device__ void stage2_group(int nb, int sz, int gtid, int gnt, int bar, Rec* re
   }
 }
 
+// Stage-2 records of neighbourhood nb, by the whole CTA: every block's
+// candidate with a negative delta becomes a kUndec record keyed
+// (delta, block), with its move in ij (i | j << 16) and its conflict interval
+// (2-opt, Or-opt) or endpoints (swap) in ab; the other blocks get kNone.
+__device__ void stage2_records(const JobDev* J, int nb, int sz, Rec* rec, uint32_t* ij) {
+  const int m = nb_blocks(nb, sz), off = nb_offset(nb, sz);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const uint64_t* keys = J->keys + off;
+  constexpr int U = 4;
+  for (int x0 = 0; x0 < m; x0 += U * nt) {
+    uint64_t kv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int x = x0 + u * nt + tid;
+      kv[u] = x < m ? keys[x] : kKeyNone;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int x = x0 + u * nt + tid;
+      if (x >= m) continue;
+      Rec r;
+      r.key = kKeyNone;
+      r.ab = 0;
+      r.st = kNone;
+      if (kv[u] != kKeyNone) {
+        const int64_t cost = key_cost(kv[u], kCtxBits);
+        if (cost < 0) {
+          int i, j;
+          map_move(nb, sz, x, (int)(kv[u] & ((1u << kCtxBits) - 1)), i, j);
+          r.key = make_key(cost, (uint32_t)x, kCtxBits);
+          ij[x] = (uint32_t)i | ((uint32_t)j << 16);
+          if (nb == 0) {
+            r.ab = (uint32_t)i | ((uint32_t)j << 16);
+          } else {
+            int a, b;
+            conflict_interval(nb, i, j, a, b);
+            r.ab = (uint32_t)a | ((uint32_t)b << 16);
+          }
+          r.st = kUndec;
+        }
+      }
+      rec[x] = r;
+    }
+  }
+}
+
 __device__ __forceinline__ int id_of(uint64_t key3) { return (int)((key3 >> kCtxBits) & 7); }
+
+// Stage 3 (cross-neighbourhood greedy with canMerge, mlkernel.cu:649-864 with
+// a stable order), the parallel apply of the selected moves (footprints are
+// disjoint for every pair canMerge accepts), statistics, the ADS prefix
+// rebuild and the candidate-key reset, by one whole CTA on the list
+// key3 / shp3 / ij3 / st3[0, m3) of kept stage-2 moves (any order; every
+// st3 entry kUndec).  t_old holds the current tour; bits, owner and t_new are
+// workspace (bits: min(m3, kBitMax)^2 bits).
+template <bool WIDE>
+__device__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* key3, const uint64_t* shp3,
+                             const uint32_t* ij3, volatile uint8_t* st3, uint32_t* bits, int32_t* owner,
+                             int32_t* t_old, int32_t* t_new) {
+  __shared__ uint32_t s_in[kBitMax / 32], s_und[kBitMax / 32];
+  __shared__ int s_ns;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  int32_t* tour = J->tour;
+  if (tid == 0) s_ns = 0;
+  __syncthreads();
+  if (m3 <= kBitMax) {
+    // conflict rows: bit y of row x <=> y precedes x and !canMerge(y, x)
+    const int W3 = (m3 + 31) >> 5;
+    for (int x = wid; x < m3; x += nw) {
+      const uint64_t kx = key3[x], sx = shp3[x];
+#pragma unroll 4
+      for (int w = 0; w < W3; w++) {
+        const int y = 32 * w + lane;
+        bool c = false;
+        if (y < m3) c = key3[y] < kx && shapes_conflict(shp3[y], sx);
+        const uint32_t word = __ballot_sync(kFull, c);
+        if (lane == 0) bits[x * W3 + w] = word;
+      }
+    }
+    for (int w = tid; w < W3; w += nt) {
+      s_in[w] = 0;
+      const int rem = m3 - 32 * w;
+      s_und[w] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+    }
+    __syncthreads();
+    for (int round = 0; round <= m3; round++) {
+      int any = 0;
+      for (int x = tid; x < m3; x += nt) {
+        if (st3[x] != kUndec) continue;
+        uint32_t hin = 0, hund = 0;
+        for (int w = 0; w < W3; w++) {
+          const uint32_t r = bits[x * W3 + w];
+          hin |= r & s_in[w];
+          hund |= r & s_und[w];
+        }
+        if (hin) st3[x] = kOut;
+        else if (!hund) st3[x] = kIn;
+        else any = 1;
+      }
+      __syncthreads();
+      for (int w = wid; w < W3; w += nw) {
+        const int x = 32 * w + lane;
+        const uint8_t sx = x < m3 ? st3[x] : kNone;
+        const uint32_t bi = __ballot_sync(kFull, sx == kIn), bu = __ballot_sync(kFull, sx == kUndec);
+        if (lane == 0) {
+          s_in[w] = bi;
+          s_und[w] = bu;
+        }
+      }
+      if (!__syncthreads_or(any)) break;
+    }
+  } else {
+    // long lists: one warp per undecided move scans the earlier ones
+    for (int round = 0; round <= m3; round++) {
+      int any = 0;
+      for (int x = wid; x < m3; x += nw) {
+        if (st3[x] != kUndec) continue;
+        const uint64_t kx = key3[x], sx = shp3[x];
+        bool out = false, blocked = false;
+        for (int y0 = 0; y0 < m3; y0 += 32) {
+          const int y = y0 + lane;
+          bool cin = false, cund = false;
+          if (y < m3) {
+            const uint64_t ky = key3[y];
+            const uint8_t sy = st3[y];
+            if (ky < kx && (sy == kUndec || sy == kIn) && shapes_conflict(shp3[y], sx)) {
+              cin = sy == kIn;
+              cund = sy == kUndec;
+            }
+          }
+          out |= __any_sync(kFull, cin);
+          blocked |= __any_sync(kFull, cund);
+          if (out) break;
+        }
+        if (lane == 0) {
+          if (out) st3[x] = kOut;
+          else if (!blocked) st3[x] = kIn;
+        }
+        if (!out && blocked) any = 1;
+      }
+      if (!__syncthreads_or(any)) break;
+    }
+  }
+  // ---- apply: every position learns which selected move (if any) owns it ----
+  for (int p = tid; p < sz; p += nt) owner[p] = -1;
+  __syncthreads();
+  for (int x = wid; x < m3; x += nw) {
+    if (st3[x] != kIn) continue;
+    const int id = id_of(key3[x]);
+    const int i = (int)(ij3[x] & 0xffff), j = (int)(ij3[x] >> 16);
+    if (id == 0) {
+      if (lane == 0) owner[i] = x;
+      if (lane == 1) owner[j] = x;
+    } else {
+      int f0, f1;
+      move_footprint(id, i, j, f0, f1);
+      for (int p = f0 + lane; p <= f1; p += 32) owner[p] = x;
+    }
+    if (lane == 0) atomicAdd(&s_ns, 1);
+  }
+  __syncthreads();
+  for (int p = tid; p < sz; p += nt) {
+    const int o = owner[p];
+    int32_t v = t_old[p];
+    if (o >= 0) v = t_old[move_source(id_of(key3[o]), (int)(ij3[o] & 0xffff), (int)(ij3[o] >> 16), p)];
+    t_new[p] = v;
+    tour[p] = v;
+  }
+  const int ns = s_ns;
+  // Applied moves in (delta, neighbourhood, block) order, for callers that
+  // ask for them (the legacy bestNeighbor move vectors).
+  if (J->moves_out != nullptr && (J->flags & kFlagRecordMoves)) {
+    for (int x = tid; x < m3; x += nt) {
+      if (st3[x] != kIn) continue;
+      int rank3 = 0;
+      for (int y = 0; y < m3; y++)
+        if (st3[y] == kIn && key3[y] < key3[x]) rank3++;
+      if (rank3 < J->moves_cap) {
+        const uint32_t id = (uint32_t)id_of(key3[x]);
+        const uint32_t i = ij3[x] & 0xffff, j = ij3[x] >> 16;
+        J->moves_out[rank3] = id | (i << 4) | (j << 18);
+        J->moves_cost[rank3] = key_cost(key3[x], kCtxBits + 3);
+      }
+    }
+  }
+  if (tid == 0) {
+    unsigned long long* stt = (unsigned long long*)J->stats;
+    atomicAdd(&stt[kStatSweeps], 1ull);
+    atomicExch(&stt[kStatLastMoves], (unsigned long long)ns);
+    atomicAdd(&stt[kStatMoves], (unsigned long long)ns);
+    if (ns > 0) atomicAdd(&stt[kStatIters], 1ull);
+    else atomicExch(&stt[kStatConverged], 1ull);
+  }
+  __syncthreads();
+  cta_prepare<WIDE>(J, t_new, t_old);  // t_old is free again: w staging
+  cta_reset_keys(J);
+}
 
 // One cluster of six CTAs per job.  CTAs 0..4 run stage 2 of neighbourhood
 // 0..4 with the whole CTA and hand their kept moves straight to CTA 5 (the
@@ -661,9 +858,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     k_merge(const JobDev* __restrict__ jobs, int use_smem) {
   extern __shared__ __align__(16) uint8_t dsm[];
   __shared__ uint64_t s_gmin[64];  // two step buffers of one entry per warp
-  __shared__ int s_m3, s_ns, s_cnt;
+  __shared__ int s_m3, s_cnt;
   __shared__ int s_flag[kNumNb];  // leader: count + 1 published by each stage-2 CTA
-  __shared__ uint32_t s_in[kBitMax / 32], s_und[kBitMax / 32];
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const JobDev* J = jobs + blockIdx.x / kClusterCtas;
@@ -672,7 +868,6 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;  // the whole cluster
   }
   const int sz = J->size, mask = J->nb_mask, tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
   const MergeLayout lay(sz);
   // Workspace of this CTA, and the leader's stage-3 lists as seen from here.
   uint8_t* ws = use_smem ? dsm : (J->ws + (size_t)rank * lay.total);
@@ -689,7 +884,6 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   int32_t* t_new = (int32_t*)(ws + lay.o_tnew);
   if (leader) {
     if (tid < kNumNb) s_flag[tid] = 0;
-    if (tid == 0) s_ns = 0;
     __syncthreads();
     cluster_arrive_release();  // the flags are initialised
     for (int p = tid; p < sz; p += nt) t_old[p] = tour[p];  // completes while stage 2 runs
@@ -698,46 +892,10 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     const int nb = rank;
     int count = 0;
     if ((mask >> nb) & 1) {
-      const int m = nb_blocks(nb, sz), off = nb_offset(nb, sz);
+      const int m = nb_blocks(nb, sz);
       Rec* rec = (Rec*)ws;
       uint32_t* ij = (uint32_t*)(ws + lay.o_ij2);
-      const uint64_t* keys = J->keys + off;
-      constexpr int U = 4;
-      for (int x0 = 0; x0 < m; x0 += U * kMergeThreads) {
-        uint64_t kv[U];
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          const int x = x0 + u * kMergeThreads + tid;
-          kv[u] = x < m ? keys[x] : kKeyNone;
-        }
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          const int x = x0 + u * kMergeThreads + tid;
-          if (x >= m) continue;
-          Rec r;
-          r.key = kKeyNone;
-          r.ab = 0;
-          r.st = kNone;
-          if (kv[u] != kKeyNone) {
-            const int64_t cost = key_cost(kv[u], kCtxBits);
-            if (cost < 0) {
-              int i, j;
-              map_move(nb, sz, x, (int)(kv[u] & ((1u << kCtxBits) - 1)), i, j);
-              r.key = make_key(cost, (uint32_t)x, kCtxBits);
-              ij[x] = (uint32_t)i | ((uint32_t)j << 16);
-              if (nb == 0) {
-                r.ab = (uint32_t)i | ((uint32_t)j << 16);
-              } else {
-                int a, b;
-                conflict_interval(nb, i, j, a, b);
-                r.ab = (uint32_t)a | ((uint32_t)b << 16);
-              }
-              r.st = kUndec;
-            }
-          }
-          rec[x] = r;
-        }
-      }
+      stage2_records(J, nb, sz, rec, ij);
       if (tid == 0) s_cnt = 0;
       __syncthreads();
       stage2_group(nb, sz, tid, nt, 1, rec, (uint64_t*)(ws + lay.o_tab), s_gmin);
@@ -828,140 +986,103 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     if (tid == 0) s_m3 = cbase[kNumNb];
     __syncthreads();
   }
-  const int m3 = s_m3;
-  uint32_t* bits = (uint32_t*)(ws + lay.o_bits);
-  if (m3 <= kBitMax) {
-    // conflict rows: bit y of row x <=> y precedes x and !canMerge(y, x)
-    const int W3 = (m3 + 31) >> 5;
-    for (int x = wid; x < m3; x += nw) {
-      const uint64_t kx = key3[x], sx = shp3[x];
-#pragma unroll 4
-      for (int w = 0; w < W3; w++) {
-        const int y = 32 * w + lane;
-        bool c = false;
-        if (y < m3) c = key3[y] < kx && shapes_conflict(shp3[y], sx);
-        const uint32_t word = __ballot_sync(kFull, c);
-        if (lane == 0) bits[x * W3 + w] = word;
-      }
-    }
-    for (int w = tid; w < W3; w += nt) {
-      s_in[w] = 0;
-      const int rem = m3 - 32 * w;
-      s_und[w] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
-    }
+  merge_finish<WIDE>(J, sz, s_m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits),
+                    (int32_t*)(ws + lay.o_owner), t_old, t_new);
+}
+
+// --------------------------------------------------------------------------
+// Throughput merge: one CTA per job.  The five stage-2 passes run one after
+// the other on the whole CTA and append their kept moves to the stage-3 list;
+// merge_finish then does the rest.  A job uses one CTA of one SM (several jobs
+// share an SM) instead of a six-SM cluster: for sets of many jobs the merge
+// throughput matters, not one job's latency.  Same moves, same order of
+// application, same results as k_merge.
+// --------------------------------------------------------------------------
+constexpr int kSoloThreads = 512;
+
+struct SoloLayout {
+  int m3cap, mmax;
+  size_t o_key3, o_shp3, o_ij3, o_st3, o_rec, o_ij2, o_tab, o_bits, o_owner, o_told, o_tnew, total;
+  __host__ __device__ explicit SoloLayout(int size) {
+    const MergeLayout ml(size);
+    m3cap = ml.m3cap;
+    mmax = ml.mmax;
+    o_key3 = 0;
+    o_shp3 = o_key3 + align_up((size_t)m3cap * 8, 16);
+    o_ij3 = o_shp3 + align_up((size_t)m3cap * 8, 16);
+    o_st3 = o_ij3 + align_up((size_t)m3cap * 4, 16);
+    const size_t u = o_st3 + align_up((size_t)m3cap, 16);
+    // stage 2 (dead once the list is complete)
+    o_rec = u;
+    o_ij2 = o_rec + align_up((size_t)mmax * sizeof(Rec), 16);
+    o_tab = o_ij2 + align_up((size_t)mmax * 4, 16);
+    const size_t e2 = o_tab + align_up((size_t)3 * (size + 4) * 8, 16);
+    // stage 3 and apply, over the same bytes
+    const size_t b = m3cap < kBitMax ? (size_t)m3cap : (size_t)kBitMax;
+    o_bits = u;
+    o_owner = o_bits + align_up(b * ((b + 31) / 32) * 4, 16);
+    o_told = o_owner + align_up((size_t)size * 4, 16);
+    o_tnew = o_told + align_up((size_t)size * 4, 16);
+    const size_t e3 = o_tnew + align_up((size_t)size * 4, 16);
+    total = align_up(e2 > e3 ? e2 : e3, 128);
+  }
+};
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __restrict__ jobs, int use_smem) {
+  extern __shared__ __align__(16) uint8_t dsm[];
+  __shared__ uint64_t s_gmin[64];
+  __shared__ int s_m3;
+  const JobDev* J = jobs + blockIdx.x;
+  {
+    const int64_t* stt = J->stats;
+    if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;
+  }
+  const int sz = J->size, mask = J->nb_mask, tid = threadIdx.x, nt = blockDim.x;
+  const SoloLayout lay(sz);
+  uint8_t* ws = use_smem ? dsm : J->ws;
+  uint64_t* key3 = (uint64_t*)(ws + lay.o_key3);
+  uint64_t* shp3 = (uint64_t*)(ws + lay.o_shp3);
+  uint32_t* ij3 = (uint32_t*)(ws + lay.o_ij3);
+  volatile uint8_t* st3 = (volatile uint8_t*)(ws + lay.o_st3);
+  Rec* rec = (Rec*)(ws + lay.o_rec);
+  uint32_t* ij = (uint32_t*)(ws + lay.o_ij2);
+  if (tid == 0) s_m3 = 0;
+  __syncthreads();
+  for (int nb = 0; nb < kNumNb; nb++) {
+    if (!((mask >> nb) & 1)) continue;
+    const int m = nb_blocks(nb, sz);
+    stage2_records(J, nb, sz, rec, ij);
     __syncthreads();
-    for (int round = 0; round <= m3; round++) {
-      int any = 0;
-      for (int x = tid; x < m3; x += nt) {
-        if (st3[x] != kUndec) continue;
-        uint32_t hin = 0, hund = 0;
-        for (int w = 0; w < W3; w++) {
-          const uint32_t r = bits[x * W3 + w];
-          hin |= r & s_in[w];
-          hund |= r & s_und[w];
-        }
-        if (hin) st3[x] = kOut;
-        else if (!hund) st3[x] = kIn;
-        else any = 1;
+    stage2_group(nb, sz, tid, nt, 1, rec, (uint64_t*)(ws + lay.o_tab), s_gmin);
+    __syncthreads();
+    int nmine = 0;
+    for (int x = tid; x < m; x += nt) nmine += rec[x].st == kIn;
+    int slot = nmine ? atomicAdd(&s_m3, nmine) : 0;
+    for (int x = tid; x < m; x += nt) {
+      if (rec[x].st != kIn) continue;
+      if (slot < lay.m3cap) {
+        const uint32_t ijx = ij[x];
+        key3[slot] = make_key(key_cost(rec[x].key, kCtxBits), ((uint32_t)nb << kCtxBits) | (uint32_t)x,
+                              kCtxBits + 3);
+        shp3[slot] = move_shape(nb, (int)(ijx & 0xffff), (int)(ijx >> 16));
+        ij3[slot] = ijx;
+        st3[slot] = kUndec;
       }
-      __syncthreads();
-      for (int w = wid; w < W3; w += nw) {
-        const int x = 32 * w + lane;
-        const uint8_t sx = x < m3 ? st3[x] : kNone;
-        const uint32_t bi = __ballot_sync(kFull, sx == kIn), bu = __ballot_sync(kFull, sx == kUndec);
-        if (lane == 0) {
-          s_in[w] = bi;
-          s_und[w] = bu;
-        }
-      }
-      if (!__syncthreads_or(any)) break;
+      slot++;
     }
-  } else {
-    // long lists: one warp per undecided move scans the earlier ones
-    for (int round = 0; round <= m3; round++) {
-      int any = 0;
-      for (int x = wid; x < m3; x += nw) {
-        if (st3[x] != kUndec) continue;
-        const uint64_t kx = key3[x], sx = shp3[x];
-        bool out = false, blocked = false;
-        for (int y0 = 0; y0 < m3; y0 += 32) {
-          const int y = y0 + lane;
-          bool cin = false, cund = false;
-          if (y < m3) {
-            const uint64_t ky = key3[y];
-            const uint8_t sy = st3[y];
-            if (ky < kx && (sy == kUndec || sy == kIn) && shapes_conflict(shp3[y], sx)) {
-              cin = sy == kIn;
-              cund = sy == kUndec;
-            }
-          }
-          out |= __any_sync(kFull, cin);
-          blocked |= __any_sync(kFull, cund);
-          if (out) break;
-        }
-        if (lane == 0) {
-          if (out) st3[x] = kOut;
-          else if (!blocked) st3[x] = kIn;
-        }
-        if (!out && blocked) any = 1;
-      }
-      if (!__syncthreads_or(any)) break;
-    }
+    __syncthreads();  // rec and ij are rebuilt for the next neighbourhood
   }
-  // ---- apply: every position learns which selected move (if any) owns it ----
-  int32_t* owner = (int32_t*)(ws + lay.o_owner);
-  for (int p = tid; p < sz; p += nt) owner[p] = -1;
+  int m3 = s_m3;
+  if (m3 > lay.m3cap) {
+    if (tid == 0) J->stats[kStatError] = 3;
+    m3 = lay.m3cap;
+  }
+  int32_t* t_old = (int32_t*)(ws + lay.o_told);
+  for (int p = tid; p < sz; p += nt) t_old[p] = J->tour[p];
   __syncthreads();
-  for (int x = wid; x < m3; x += nw) {
-    if (st3[x] != kIn) continue;
-    const int id = id_of(key3[x]);
-    const int i = (int)(ij3[x] & 0xffff), j = (int)(ij3[x] >> 16);
-    if (id == 0) {
-      if (lane == 0) owner[i] = x;
-      if (lane == 1) owner[j] = x;
-    } else {
-      int f0, f1;
-      move_footprint(id, i, j, f0, f1);
-      for (int p = f0 + lane; p <= f1; p += 32) owner[p] = x;
-    }
-    if (lane == 0) atomicAdd(&s_ns, 1);
-  }
-  __syncthreads();
-  for (int p = tid; p < sz; p += nt) {
-    const int o = owner[p];
-    int32_t v = t_old[p];
-    if (o >= 0) v = t_old[move_source(id_of(key3[o]), (int)(ij3[o] & 0xffff), (int)(ij3[o] >> 16), p)];
-    t_new[p] = v;
-    tour[p] = v;
-  }
-  const int ns = s_ns;
-  // Applied moves in (delta, neighbourhood, block) order, for callers that
-  // ask for them (the legacy bestNeighbor move vectors).
-  if (J->moves_out != nullptr && (J->flags & kFlagRecordMoves)) {
-    for (int x = tid; x < m3; x += nt) {
-      if (st3[x] != kIn) continue;
-      int rank3 = 0;
-      for (int y = 0; y < m3; y++)
-        if (st3[y] == kIn && key3[y] < key3[x]) rank3++;
-      if (rank3 < J->moves_cap) {
-        const uint32_t id = (uint32_t)id_of(key3[x]);
-        const uint32_t i = ij3[x] & 0xffff, j = ij3[x] >> 16;
-        J->moves_out[rank3] = id | (i << 4) | (j << 18);
-        J->moves_cost[rank3] = key_cost(key3[x], kCtxBits + 3);
-      }
-    }
-  }
-  if (tid == 0) {
-    unsigned long long* stt = (unsigned long long*)J->stats;
-    atomicAdd(&stt[kStatSweeps], 1ull);
-    atomicExch(&stt[kStatLastMoves], (unsigned long long)ns);
-    atomicAdd(&stt[kStatMoves], (unsigned long long)ns);
-    if (ns > 0) atomicAdd(&stt[kStatIters], 1ull);
-    else atomicExch(&stt[kStatConverged], 1ull);
-  }
-  __syncthreads();
-  cta_prepare<WIDE>(J, t_new, t_old);  // t_old is free again: w staging
-  cta_reset_keys(J);
+  merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
+                     t_old, (int32_t*)(ws + lay.o_tnew));
 }
 
 // --------------------------------------------------------------------------
@@ -1131,7 +1252,20 @@ cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* job
 }  // namespace
 
 size_t merge_smem_bytes(int size) { return MergeLayout(size).total; }
-size_t merge_ws_bytes(int size) { return MergeLayout(size).total * kClusterCtas; }
+size_t merge_ws_bytes(int size) {
+  const size_t c = MergeLayout(size).total * kClusterCtas, o = SoloLayout(size).total;
+  return c > o ? c : o;
+}
+size_t solo_smem_bytes(int size) { return SoloLayout(size).total; }
+int solo_smem_max_size() {
+  static int cached = 0;
+  if (cached == 0) {
+    int sz = 8;
+    while (sz < kMaxSize && SoloLayout(sz + 1).total <= (size_t)(227 * 1024 - 8192)) sz++;
+    cached = sz;
+  }
+  return cached;
+}
 int merge_smem_max_size() {
   // Largest size whose merge workspace fits the 227 KB opt-in shared memory
   // (minus the kernel's static shared memory).
@@ -1182,7 +1316,12 @@ cudaError_t configure_merge(size_t bytes) {
   bytes = bytes > MergeLayout(merge_smem_max_size()).total ? bytes : MergeLayout(merge_smem_max_size()).total;
   cudaError_t e = cudaFuncSetAttribute(k_merge<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_merge<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  e = cudaFuncSetAttribute(k_merge<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  const int solo = (int)SoloLayout(solo_smem_max_size()).total;
+  e = cudaFuncSetAttribute(k_merge_solo<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_merge_solo<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
 }
 
 cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
@@ -1191,6 +1330,15 @@ cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem
   const size_t smem = use_smem ? MergeLayout(max_size).total : 0;
   if (wide) k_merge<true><<<njobs * kClusterCtas, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
   else k_merge<false><<<njobs * kClusterCtas, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
+                              cudaStream_t s) {
+  if (njobs <= 0) return cudaSuccess;
+  const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
+  if (wide) k_merge_solo<true><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  else k_merge_solo<false><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -23,6 +23,14 @@ size_t merge_smem_bytes(int size);
 size_t merge_ws_bytes(int size);
 // Largest size whose merge workspace fits in shared memory.
 int merge_smem_max_size();
+// The same for the one-CTA-per-job merge (launch_merge_solo).
+size_t solo_smem_bytes(int size);
+int solo_smem_max_size();
+// A job of `size` needs a global merge workspace (some merge kernel cannot
+// run it from shared memory).
+inline bool merge_needs_ws(int size) {
+  return size > merge_smem_max_size() || size > solo_smem_max_size();
+}
 
 // Opt the merge kernels into `bytes` of dynamic shared memory (call before
 // launching or capturing merges that use shared memory).
@@ -41,8 +49,12 @@ cudaError_t launch_prepare(const JobDev* jobs, int njobs, bool wide, bool reset_
 // merge ignores the others); false publishes every block's best (evaluation).
 cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
                          int shape, bool improve_only, cudaStream_t s);
+// One six-CTA cluster per job (latency: a single job or a few).
 cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
                          cudaStream_t s);
+// One CTA per job (throughput: sets of many jobs).  Identical results.
+cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
+                              cudaStream_t s);
 // Reference ADS buffer (source/mlads.h:38-74) of each job's current tour.
 cudaError_t launch_ads(const JobDev* job, const int32_t* cx, const int32_t* cy, uint32_t* ads,
                        int cost_tour, int dist_round, cudaStream_t s, uint32_t* Pbuf, int size);

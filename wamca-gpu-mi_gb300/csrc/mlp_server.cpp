@@ -10,8 +10,10 @@
 //      and the ADS prefix arrays are prepared, with no host synchronisation;
 //   2. runs `iters` DVND iterations over every admitted search in shared
 //      launches: one sweep over all searches' tiles, then one merge launch for
-//      the searches whose merge fits shared memory and one for the rest.  A
-//      search that converged or used its sweep limit turns into no-op CTAs;
+//      the searches whose merge fits shared memory and one for the rest (one
+//      CTA per search when many are active, a six-CTA cluster per search
+//      otherwise).  A search that converged or used its sweep limit turns
+//      into no-op CTAs;
 //   3. reads every slot's statistics (one copy) and retires the finished
 //      searches: tour and statistics become the request's result, the memory
 //      returns to the pool in stream order and the slot is free again.
@@ -275,7 +277,7 @@ static int server_step(mlp_server* s, int iters) {
 
   // 2. Iterations over every admitted search: searches whose merge fits
   //    shared memory first, the rest (global merge workspace) after them.
-  const int smem_max = merge_smem_max_size();
+  const int smem_max = std::min(merge_smem_max_size(), solo_smem_max_size());
   std::stable_sort(s->active.begin(), s->active.end(), [smem_max](const Active& a, const Active& b) {
     return (a.job->size > smem_max) < (b.job->size > smem_max);
   });
@@ -315,9 +317,15 @@ static int server_step(mlp_server* s, int iters) {
              "copy tiles");
     for (int it = 0; it < iters; it++) {
       MLP_CUDA(launch_sweep(s->dtiles, (int)t, s->djobs, s->wide, shape, true, s->stream), "sweep kernel");
-      MLP_CUDA(launch_merge(s->djobs, ksmall, s->wide, true, max_small, s->stream), "merge kernel");
-      MLP_CUDA(launch_merge(s->djobs + ksmall, nact - ksmall, s->wide, false, max_large, s->stream),
-               "merge kernel");
+      if (nact >= kSoloMinJobs) {
+        MLP_CUDA(launch_merge_solo(s->djobs, ksmall, s->wide, true, max_small, s->stream), "merge kernel");
+        MLP_CUDA(launch_merge_solo(s->djobs + ksmall, nact - ksmall, s->wide, false, max_large, s->stream),
+                 "merge kernel");
+      } else {
+        MLP_CUDA(launch_merge(s->djobs, ksmall, s->wide, true, max_small, s->stream), "merge kernel");
+        MLP_CUDA(launch_merge(s->djobs + ksmall, nact - ksmall, s->wide, false, max_large, s->stream),
+                 "merge kernel");
+      }
     }
   }
 

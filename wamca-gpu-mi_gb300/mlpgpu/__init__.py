@@ -117,6 +117,7 @@ def lib() -> C.CDLL:
         "mlp_batch_destroy": (None, [vp]),
         "mlp_batch_set_stream": (C.c_int, [vp, vp]),
         "mlp_batch_set_tile_shape": (C.c_int, [vp, i32]),
+        "mlp_batch_set_merge_mode": (C.c_int, [vp, i32]),
         "mlp_batch_add": (C.c_int, [vp, vp, vp, i32, P(i32)]),
         "mlp_batch_run": (C.c_int, [vp, i32, i32]),
         "mlp_batch_reset": (C.c_int, [vp]),
@@ -375,6 +376,10 @@ class Batch:
 
     def set_tile_shape(self, shape: int) -> None:
         _check(lib().mlp_batch_set_tile_shape(self._h, shape))
+
+    def set_merge_mode(self, mode: int) -> None:
+        """0 automatic, 1 six-CTA cluster per job, 2 one CTA per job."""
+        _check(lib().mlp_batch_set_merge_mode(self._h, mode))
 
     def add(self, problem: Problem, tour: Sequence[int]) -> int:
         t = _i32(tour)

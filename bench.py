@@ -602,6 +602,11 @@ def run_ours(args, world, rank, local) -> None:
                      "peak_source": peaks["source"] + " hbm_gbs (STREAM copy)"},
         "clocks": P["clocks"],
         "gpu_launches": launches,
+        "kernel_shares": {"note": "device-time shares of one DVND iteration from the ncu launch list "
+                                  "(profiles/dvnd_n1000_launches.md); the roofline above is the sweep's, the "
+                                  "bandwidth kernel; the merge is latency-bound (critical path of the greedy "
+                                  "rounds and barriers, 0.6 MB of traffic)",
+                          "k_merge": 0.631, "k_sweep": 0.354},
     }
     line.update(extra)
     if not args.no_cpu:

@@ -202,6 +202,9 @@ MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape);
  * 16 jobs or more, otherwise a six-CTA cluster per job), 1 = cluster, 2 = one
  * CTA per job.  Every mode gives the same results. */
 MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode);
+/* Iterations between the host's convergence checks (default 16); after each
+ * check the jobs that converged leave the launches. */
+MLP_API int mlp_batch_set_check_interval(mlp_batch_t b, int32_t iterations);
 
 /* ---- serving form: continuous batching of arriving searches ----
  * A server owns a CUDA stream and a device memory pool.  Requests (instance

@@ -496,6 +496,14 @@ MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape) {
   return kOk;
 }
 
+MLP_API int mlp_batch_set_check_interval(mlp_batch_t b, int32_t iterations) {
+  if (!b) return arg_error("null batch");
+  if (iterations < 1 || iterations > 256) return arg_error("check interval must lie in [1, 256]");
+  b->check_interval = iterations;
+  if (b->set) return b->set->set_unroll(iterations);
+  return kOk;
+}
+
 MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode) {
   if (!b) return arg_error("null batch");
   if (mode < kMergeAuto || mode > kMergeSolo) return arg_error("merge mode must be 0, 1 or 2");
@@ -533,6 +541,7 @@ static int batch_build(mlp_batch* b) {
   b->set.reset(new JobSet(js, b->wide, b->stream));
   if (b->shape >= 0) MLP_TRY(b->set->set_shape(b->shape));
   MLP_TRY(b->set->set_merge_mode(b->merge_mode));
+  MLP_TRY(b->set->set_unroll(b->check_interval));
   MLP_TRY(b->set->init());
   return batch_upload(b);
 }

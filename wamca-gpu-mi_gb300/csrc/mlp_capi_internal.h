@@ -24,6 +24,7 @@ struct mlp_batch {
   int shape = -1;
   int mask = 0x1f;
   int merge_mode = 0;
+  int check_interval = 16;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<mlp::Job>> jobs;

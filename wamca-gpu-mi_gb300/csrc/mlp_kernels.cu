@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   const C* __restrict__ W = (const C*)J->W;
   const C* __restrict__ Q = (const C*)J->Q;
   // Loaded with the tile's other independent loads; a job that converged or
-  // used its sweep limit is skipped after the staging barriers.
+  // used its sweep limit is skipped before its distance gathers.
   const bool done = stats[kStatConverged] || stats[kStatSweeps] >= stats[kStatLimit];
 
   for (int q = tid; q < SR; q += TL) {
@@ -278,6 +278,7 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
     for (int k = 0; k < 3; k++) sCA[k][q] = ok ? Ag[k * pad + p] : 0;
   }
   __syncthreads();
+  if (done) return;
   {
     // All gathers of the tile are issued before any is stored, so their
     // latencies overlap (one L2/HBM round trip per tile instead of one per load).
@@ -304,7 +305,6 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
     }
   }
   __syncthreads();
-  if (done) return;
 
   uint64_t* keys = J->keys;
   const int L = L0 + tid, b = tid + 1, lane = tid & 31;

@@ -118,6 +118,7 @@ def lib() -> C.CDLL:
         "mlp_batch_set_stream": (C.c_int, [vp, vp]),
         "mlp_batch_set_tile_shape": (C.c_int, [vp, i32]),
         "mlp_batch_set_merge_mode": (C.c_int, [vp, i32]),
+        "mlp_batch_set_check_interval": (C.c_int, [vp, i32]),
         "mlp_batch_add": (C.c_int, [vp, vp, vp, i32, P(i32)]),
         "mlp_batch_run": (C.c_int, [vp, i32, i32]),
         "mlp_batch_reset": (C.c_int, [vp]),
@@ -380,6 +381,10 @@ class Batch:
     def set_merge_mode(self, mode: int) -> None:
         """0 automatic, 1 six-CTA cluster per job, 2 one CTA per job."""
         _check(lib().mlp_batch_set_merge_mode(self._h, mode))
+
+    def set_check_interval(self, iterations: int) -> None:
+        """Iterations between convergence checks (converged jobs then leave the launches)."""
+        _check(lib().mlp_batch_set_check_interval(self._h, iterations))
 
     def add(self, problem: Problem, tour: Sequence[int]) -> int:
         t = _i32(tour)

@@ -108,8 +108,8 @@ MLP_API int mlp_solver_create(mlp_problem_t p, int32_t wide, mlp_solver_t* out);
 MLP_API void mlp_solver_destroy(mlp_solver_t s);
 /* Stream on which every later call of this solver runs (NULL: the solver's own). */
 MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
-/* Sweep tile shape index (0..7: diagonals x rows = 32x4, 32x8, 32x16, 64x4, 64x8,
- * 64x16, 128x8, 128x16).  Loop mode of mlp_solver_dvnd: iterations >= 1
+/* Sweep tile shape index (0..9: diagonals x rows = 32x4, 32x8, 32x16, 64x4, 64x8,
+ * 64x16, 128x8, 128x16, 32x32, 64x32).  Loop mode of mlp_solver_dvnd: iterations >= 1
  * (default 16) replays CUDA graphs of that many iterations and checks
  * convergence on the host in between; iterations = 0 runs the whole loop on
  * the device (a CUDA-graph while node, no host round trips; always the mode
@@ -160,6 +160,19 @@ MLP_API int mlp_solver_stats(mlp_solver_t s, mlp_dvnd_stats_t* stats);
  * one ADS rebuild.  *evals_per_sweep = move evaluations of one sweep. */
 MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats,
                              int64_t* evals_per_sweep);
+/* Tile-shape table (no counterpart in the reference; chosen by the
+ * autotuner wamca-gpu-mi_gb300/mlpgpu/autotune.py).  Row q applies to job
+ * sets whose largest tour has at most max_size[q] positions: shape_one[q] for
+ * fewer than 8 jobs, shape_many[q] for 8 or more; sizes strictly increasing,
+ * count <= 64 (0 clears the table; without a table a built-in rule applies).
+ * Process-wide; used by solvers, batches and servers created afterwards (an
+ * explicit set_tile_shape wins).  The shape never changes results. */
+MLP_API int mlp_tuning_set(const int32_t* max_size, const int32_t* shape_one, const int32_t* shape_many,
+                           int32_t count);
+MLP_API int mlp_tuning_get(int32_t* max_size, int32_t* shape_one, int32_t* shape_many, int32_t cap,
+                           int32_t* count);
+/* Loads the table from the autotuner's JSON file ("table": [[size, one, many], ...]). */
+MLP_API int mlp_tuning_load(const char* path);
 /* Autotune the sweep tile shape on the current tour; returns the chosen index. */
 MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape);
 

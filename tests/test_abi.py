@@ -84,3 +84,31 @@ def test_segfault_raises_sigsegv_in_a_child_process(built_lib):
             % os.path.join(ROOT, "wamca-gpu-mi_gb300"))
     r = subprocess.run(["python3", "-c", code], capture_output=True)
     assert r.returncode == -11
+
+
+def test_tuning_table_set_get_load_and_validation(tmp_path):
+    """The autotuner's tile-shape table: round trip, JSON loading (the format
+    mlpgpu/autotune.py writes) and rejection of malformed tables.  Host-only
+    calls (no GPU work)."""
+    import json
+
+    mlpgpu = pytest.importorskip("mlpgpu")
+    saved = mlpgpu.tuning_table()
+    try:
+        mlpgpu.set_tuning_table([(101, 0, 4), (1001, 3, 4), (16384, 7, 7)])
+        assert mlpgpu.tuning_table() == [(101, 0, 4), (1001, 3, 4), (16384, 7, 7)]
+        p = tmp_path / "t.json"
+        p.write_text(json.dumps({"device": "x", "table": [[201, 1, 2], [5001, 3, 7]],
+                                 "timings": [{"n": 200, "one_s": {"0": 0.1}}]}, indent=1))
+        assert mlpgpu.lib().mlp_tuning_load(str(p).encode()) == 0
+        assert mlpgpu.tuning_table() == [(201, 1, 2), (5001, 3, 7)]
+        for bad in ([(101, 0, 10)], [(1001, 0, 1), (101, 0, 1)], [(0, 0, 0)]):
+            with pytest.raises(mlpgpu.MLPError):
+                mlpgpu.set_tuning_table(bad)
+        assert mlpgpu.tuning_table() == [(201, 1, 2), (5001, 3, 7)]  # unchanged by rejected tables
+        (tmp_path / "bad.json").write_text('{"device": "x"}')
+        assert mlpgpu.lib().mlp_tuning_load(str(tmp_path / "bad.json").encode()) == 5
+        mlpgpu.set_tuning_table([])
+        assert mlpgpu.tuning_table() == []
+    finally:
+        mlpgpu.set_tuning_table(saved)

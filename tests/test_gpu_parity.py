@@ -47,7 +47,7 @@ def test_candidates_all_neighbourhoods(mlpgpu_mod, n, seed, wide):
         assert np.array_equal(i, oi) and np.array_equal(j, oj), f"nb {nb}: moves differ"
 
 
-@pytest.mark.parametrize("shape", range(8))
+@pytest.mark.parametrize("shape", range(10))
 def test_candidates_every_tile_shape(mlpgpu_mod, shape):
     n = 333
     x, y = oracle.clustered_instance(n, 11)

@@ -420,6 +420,21 @@ MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats, i
   return kOk;
 }
 
+MLP_API int mlp_tuning_set(const int32_t* max_size, const int32_t* shape_one, const int32_t* shape_many,
+                           int32_t count) {
+  return tuning_set(max_size, shape_one, shape_many, count);
+}
+
+MLP_API int mlp_tuning_get(int32_t* max_size, int32_t* shape_one, int32_t* shape_many, int32_t cap,
+                           int32_t* count) {
+  int c = 0;
+  const int st = tuning_get(max_size, shape_one, shape_many, cap, &c);
+  if (count) *count = c;
+  return st;
+}
+
+MLP_API int mlp_tuning_load(const char* path) { return tuning_load(path); }
+
 MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape) {
   if (!s) return arg_error("null solver");
   cudaStream_t st = s->set->stream();

@@ -2,6 +2,9 @@
 #include "mlp_engine.h"
 
 #include <algorithm>
+#include <cctype>
+#include <iterator>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -334,13 +337,108 @@ void job_tiles(int size, int shape, std::vector<SweepTile>* out) {
     for (int L0 = 1; r0 + L0 <= size - 2; L0 += ts.tl) out->push_back(SweepTile{0, r0, L0, 0});
 }
 
+// Tile-shape table chosen by the autotuner (mlpgpu/autotune.py): rows of
+// (largest tour size, shape for one job, shape for many jobs), ascending.
+namespace {
+std::mutex g_tune_mu;
+std::vector<std::array<int32_t, 3>> g_tune;
+}  // namespace
+
+int tuning_set(const int32_t* max_size, const int32_t* one, const int32_t* many, int count) {
+  if (count < 0 || count > 64 || (count > 0 && (!max_size || !one || !many))) {
+    set_error("tuning table: count must lie in [0, 64] with three arrays of that length");
+    return kErrArg;
+  }
+  std::vector<std::array<int32_t, 3>> t;
+  for (int q = 0; q < count; q++) {
+    if (max_size[q] < 1 || one[q] < 0 || one[q] >= kNumTileShapes || many[q] < 0 || many[q] >= kNumTileShapes) {
+      set_error("tuning table: sizes must be positive and shapes valid tile-shape indices");
+      return kErrArg;
+    }
+    if (q > 0 && max_size[q] <= max_size[q - 1]) {
+      set_error("tuning table: sizes must be strictly increasing");
+      return kErrArg;
+    }
+    t.push_back({max_size[q], one[q], many[q]});
+  }
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune.swap(t);
+  return kOk;
+}
+
+int tuning_get(int32_t* max_size, int32_t* one, int32_t* many, int cap, int* count) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  if (count) *count = (int)g_tune.size();
+  for (int q = 0; q < (int)g_tune.size() && q < cap; q++) {
+    if (max_size) max_size[q] = g_tune[q][0];
+    if (one) one[q] = g_tune[q][1];
+    if (many) many[q] = g_tune[q][2];
+  }
+  return kOk;
+}
+
+int tuning_load(const char* path) {
+  std::ifstream f(path ? path : "");
+  if (!f.is_open()) {
+    set_error(std::string("cannot open tuning table: ") + (path ? path : "(null)"));
+    return kErrIo;
+  }
+  // The integers of the "table" array, three per row ([size, one, many]).
+  std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  const size_t k = text.find("\"table\"");
+  if (k == std::string::npos) {
+    set_error("tuning table: no \"table\" key");
+    return kErrFormat;
+  }
+  const size_t open = text.find('[', k);
+  if (open == std::string::npos) {
+    set_error("tuning table: \"table\" must be a list of [size, shape_one, shape_many] rows");
+    return kErrFormat;
+  }
+  std::vector<int32_t> v;
+  int depth = 0;
+  size_t q = open;
+  for (; q < text.size(); q++) {
+    const char ch = text[q];
+    if (ch == '[') depth++;
+    else if (ch == ']' && --depth == 0) break;
+    else if (std::isdigit((unsigned char)ch)) {
+      size_t e = q;
+      while (e < text.size() && std::isdigit((unsigned char)text[e])) e++;
+      v.push_back((int32_t)std::atol(text.substr(q, e - q).c_str()));
+      q = e - 1;
+    }
+  }
+  if (depth != 0) {
+    set_error("tuning table: unterminated \"table\" list");
+    return kErrFormat;
+  }
+  if (v.empty() || v.size() % 3 != 0) {
+    set_error("tuning table: rows must hold three integers");
+    return kErrFormat;
+  }
+  std::vector<int32_t> a, b, c;
+  for (size_t q = 0; q < v.size(); q += 3) {
+    a.push_back(v[q]);
+    b.push_back(v[q + 1]);
+    c.push_back(v[q + 2]);
+  }
+  return tuning_set(a.data(), b.data(), c.data(), (int)a.size());
+}
+
 int default_shape(int size, int njobs) {
-  // Measured on GB300: one n=1000 job is latency-bound and prefers many small
-  // tiles; a set of many jobs is throughput-bound and prefers 64 x 8.
-  if (size > 2000) return 7;    // 128 diagonals x 16 rows
-  if (njobs >= 8) return 4;     // 64 x 8
-  if (size <= 400) return 0;    // 32 x 4
-  return 3;                     // 64 x 4
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (const auto& row : g_tune)
+      if (size <= row[0]) return njobs >= kManyJobs ? row[2] : row[1];
+  }
+  // Built-in rule, measured on GB300: one n=1000 job is latency-bound and
+  // prefers many small tiles; a set of many jobs is throughput-bound and
+  // prefers 64 x 8.
+  if (size > 2000) return 7;          // 128 diagonals x 16 rows
+  if (njobs >= kManyJobs) return 4;   // 64 x 8
+  if (size <= 400) return 0;          // 32 x 4
+  return 3;                           // 64 x 4
 }
 
 // ---------------------------------------------------------------- JobSet

@@ -177,7 +177,12 @@ class JobSet {
   int loop_unroll_ = 0;
 };
 
-// Sweep tile shape for a job set whose largest tour has `size` positions.
+// Sweep tile shape for a job set whose largest tour has `size` positions:
+// the autotuner's table when one is set, else a built-in rule.
 int default_shape(int size, int njobs);
+constexpr int kManyJobs = 8;  // job sets this large use the "many jobs" shape
+int tuning_set(const int32_t* max_size, const int32_t* one, const int32_t* many, int count);
+int tuning_get(int32_t* max_size, int32_t* one, int32_t* many, int cap, int* count);
+int tuning_load(const char* path);
 
 }  // namespace mlp

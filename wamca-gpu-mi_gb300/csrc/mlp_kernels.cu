@@ -282,25 +282,30 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   {
     // All gathers of the tile are issued before any is stored, so their
     // latencies overlap (one L2/HBM round trip per tile instead of one per load).
-    constexpr int NG = (SR * SC + TL - 1) / TL;
-    int32_t gv[NG];
+    // At most GB loads per thread in flight at once (bounds the registers of
+    // the tallest tiles; every other shape needs a single batch).
+    constexpr int NG = (SR * SC + TL - 1) / TL, GB = 21;
 #pragma unroll
-    for (int u = 0; u < NG; u++) {
-      const int idx = tid + u * TL;
-      int32_t v = 0;
-      if (idx < SR * SC) {
-        const int a = idx / SC, b = idx - a * SC;
-        const int rp = r0 - 1 + a, cp = rp + L0 - 1 + b;
-        if (rp <= sz - 1 && cp <= sz - 1) v = __ldg(D + (size_t)sRowT[a] * n + sColT[a + b]);
+    for (int u0 = 0; u0 < NG; u0 += GB) {
+      int32_t gv[GB];
+#pragma unroll
+      for (int u = 0; u < GB; u++) {
+        const int idx = tid + (u0 + u) * TL;
+        int32_t v = 0;
+        if (u0 + u < NG && idx < SR * SC) {
+          const int a = idx / SC, b = idx - a * SC;
+          const int rp = r0 - 1 + a, cp = rp + L0 - 1 + b;
+          if (rp <= sz - 1 && cp <= sz - 1) v = __ldg(D + (size_t)sRowT[a] * n + sColT[a + b]);
+        }
+        gv[u] = v;
       }
-      gv[u] = v;
-    }
 #pragma unroll
-    for (int u = 0; u < NG; u++) {
-      const int idx = tid + u * TL;
-      if (idx < SR * SC) {
-        const int a = idx / SC, b = idx - a * SC;
-        sS[a][b] = gv[u];
+      for (int u = 0; u < GB; u++) {
+        const int idx = tid + (u0 + u) * TL;
+        if (u0 + u < NG && idx < SR * SC) {
+          const int a = idx / SC, b = idx - a * SC;
+          sS[a][b] = gv[u];
+        }
       }
     }
   }
@@ -1245,6 +1250,8 @@ cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* job
     case 5: return sweep_launch<WIDE, 64, 16>(tiles, ntiles, jobs, improve_only, s);
     case 6: return sweep_launch<WIDE, 128, 8>(tiles, ntiles, jobs, improve_only, s);
     case 7: return sweep_launch<WIDE, 128, 16>(tiles, ntiles, jobs, improve_only, s);
+    case 8: return sweep_launch<WIDE, 32, 32>(tiles, ntiles, jobs, improve_only, s);
+    case 9: return sweep_launch<WIDE, 64, 32>(tiles, ntiles, jobs, improve_only, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -12,7 +12,8 @@ struct TileShape {
   int tl;  // diagonals per tile (= threads per CTA)
   int tr;  // rows per tile
 };
-constexpr TileShape kTileShapes[] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {64, 16}, {128, 8}, {128, 16}};
+constexpr TileShape kTileShapes[] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {64, 16}, {128, 8}, {128, 16},
+                                       {32, 32}, {64, 32}};
 constexpr int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
 
 // Bytes of dynamic shared memory the merge kernel needs for `size`

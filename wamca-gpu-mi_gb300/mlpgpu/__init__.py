@@ -21,6 +21,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libmlpgpu.so")
+TUNING_PATH = os.path.join(_HERE, "tuning_gb300.json")
 
 NB_SWAP, NB_2OPT, NB_OROPT1, NB_OROPT2, NB_OROPT3 = range(5)
 NB_ALL = 0x1F
@@ -113,6 +114,9 @@ def lib() -> C.CDLL:
         "mlp_solver_sweep": (C.c_int, [vp, i32, i32, P(i64)]),
         "mlp_solver_autotune": (C.c_int, [vp, P(i32)]),
         "mlp_eval_noalloc": (C.c_int, [vp, i32, vp, i32, i32, vp, vp, vp, vp]),
+        "mlp_tuning_set": (C.c_int, [vp, vp, vp, i32]),
+        "mlp_tuning_get": (C.c_int, [vp, vp, vp, i32, P(i32)]),
+        "mlp_tuning_load": (C.c_int, [C.c_char_p]),
         "mlp_batch_create": (C.c_int, [i32, P(vp)]),
         "mlp_batch_destroy": (None, [vp]),
         "mlp_batch_set_stream": (C.c_int, [vp, vp]),
@@ -149,7 +153,27 @@ def lib() -> C.CDLL:
         f.restype = res
         f.argtypes = args
     _lib = L
+    # The tile-shape table the autotuner measured on GB300 (shapes only: results
+    # never depend on it).
+    if os.path.exists(TUNING_PATH):
+        L.mlp_tuning_load(TUNING_PATH.encode())
     return L
+
+
+def tuning_table() -> list:
+    """Current tile-shape table: [(max tour size, shape for one job, shape for many jobs), ...]."""
+    a, b, c = (np.zeros(64, np.int32) for _ in range(3))
+    k = C.c_int32()
+    _check(lib().mlp_tuning_get(_ptr(a), _ptr(b), _ptr(c), 64, C.byref(k)))
+    return [(int(a[q]), int(b[q]), int(c[q])) for q in range(k.value)]
+
+
+def set_tuning_table(rows) -> None:
+    """Sets the tile-shape table from (max tour size, shape one, shape many) rows ([] clears it)."""
+    a = np.array([r[0] for r in rows], np.int32)
+    b = np.array([r[1] for r in rows], np.int32)
+    c = np.array([r[2] for r in rows], np.int32)
+    _check(lib().mlp_tuning_set(_ptr(a), _ptr(b), _ptr(c), len(rows)))
 
 
 def _check(status: int) -> None:

@@ -863,7 +863,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     k_merge(const JobDev* __restrict__ jobs, int use_smem) {
   extern __shared__ __align__(16) uint8_t dsm[];
   __shared__ uint64_t s_gmin[64];  // two step buffers of one entry per warp
-  __shared__ int s_m3, s_cnt;
+  __shared__ int s_m3, s_cnt, s_err;
   __shared__ int s_flag[kNumNb];  // leader: count + 1 published by each stage-2 CTA
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -934,6 +934,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   }
   // ---- leader: wait for the five neighbourhoods (bounded), then compact ----
   if (tid == 0) {
+    s_err = 0;
     long long spins = 0;
     for (;;) {
       int ready = 0;
@@ -941,6 +942,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
       if (ready == kNumNb) break;
       if (++spins > (1ll << 26)) {
         J->stats[kStatError] = 2;
+        s_err = 1;
         break;
       }
       __nanosleep(64);
@@ -948,7 +950,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   }
   __syncthreads();
   fence_acquire_cluster();
-  if (J->stats[kStatError] == 2) return;
+  if (s_err) return;
   {
     int cnt[kNumNb], cbase[kNumNb + 1];
     cbase[0] = 0;
@@ -956,26 +958,35 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
       cnt[nb] = s_flag[nb] - 1;
       cbase[nb + 1] = cbase[nb] + cnt[nb];
     }
-    // Move every region's entries to the front, chunk by chunk in increasing
-    // order (an entry only moves to a lower index, so unread ones survive).
+    // Region offsets (constant divisors once the loop is unrolled).
+    int roff[kNumNb];
+    roff[0] = 0;
+#pragma unroll
+    for (int nb = 1; nb < kNumNb; nb++) roff[nb] = roff[nb - 1] + region_cap(nb - 1, sz);
+    // Move every region's entries to the front: all loads of a chunk, a
+    // barrier, then all stores (a destination may be another region's
+    // unread source).
+    const int total = cbase[kNumNb];
     constexpr int V = 4;
-    for (int q0 = 0; q0 < lay.m3cap; q0 += V * nt) {
+    for (int g0 = 0; g0 < total; g0 += V * nt) {
       uint64_t kk[V], ss[V];
       uint32_t jj[V];
       int dst[V];
 #pragma unroll
       for (int v = 0; v < V; v++) {
-        const int q = q0 + tid + v * nt;
+        const int g = g0 + tid + v * nt;
         dst[v] = -1;
-        if (q >= lay.m3cap) continue;
-        int nb = 0;
-        while (nb + 1 < kNumNb && q >= region_off(nb + 1, sz)) nb++;
-        const int local = q - region_off(nb, sz);
-        if (local >= cnt[nb]) continue;
-        dst[v] = cbase[nb] + local;
-        kk[v] = key3[q];
-        ss[v] = shp3[q];
-        jj[v] = ij3[q];
+        if (g >= total) continue;
+        // The region holding compact index g: the last one starting at or
+        // before g (empty regions share their start with the next one).
+        int src = g;
+#pragma unroll
+        for (int q = 0; q < kNumNb; q++)
+          if (g >= cbase[q]) src = roff[q] + (g - cbase[q]);
+        dst[v] = g;
+        kk[v] = key3[src];
+        ss[v] = shp3[src];
+        jj[v] = ij3[src];
       }
       __syncthreads();
 #pragma unroll

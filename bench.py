@@ -160,26 +160,32 @@ def dist_init():
     return world, rank, local
 
 
-def reduce_max(vals: list[float], world: int) -> list[float]:
+def _reduce(vals: list[float], world: int, op: str) -> list[float]:
     if world <= 1:
         return vals
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor(vals, dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor(vals, dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return t.tolist()
+
+
+def reduce_max(vals: list[float], world: int) -> list[float]:
+    """Element-wise maximum over ranks (slowest rank's times)."""
+    return _reduce(vals, world, "max")
 
 
 def reduce_sum(vals: list[float], world: int) -> list[float]:
-    if world <= 1:
-        return vals
-    import torch
-    import torch.distributed as dist
+    """Element-wise sum over ranks (work done by the whole job)."""
+    return _reduce(vals, world, "sum")
 
-    t = torch.tensor(vals, dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return t.tolist()
+
+def shard(count: int, world: int, rank: int) -> range:
+    """Independent searches are partitioned across ranks by index (no
+    collective on the data path): rank r takes r, r + world, ..."""
+    return range(rank, count, world)
 
 
 # --------------------------------------------------------------------------- CPU

@@ -465,8 +465,8 @@ constexpr int kClusterCtas = 6;  // five stage-2 CTAs and the stage-3 leader
 //   B: swap endpoint tables (stage 2), then the stage-3 move list and bit rows
 //   T: the old and the new tour
 __host__ __device__ __forceinline__ int region_cap(int nb, int size) {
-  const int div[kNumNb] = {4, 2, 3, 4, 5};
-  return size / div[nb] + 2;
+  const int div = nb == 0 ? 4 : nb == 1 ? 2 : nb == 2 ? 3 : nb == 3 ? 4 : 5;
+  return size / div + 2;
 }
 __host__ __device__ __forceinline__ int region_off(int nb, int size) {
   int o = 0;
@@ -952,12 +952,10 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   fence_acquire_cluster();
   if (s_err) return;
   {
-    int cnt[kNumNb], cbase[kNumNb + 1];
+    int cbase[kNumNb + 1];
     cbase[0] = 0;
-    for (int nb = 0; nb < kNumNb; nb++) {
-      cnt[nb] = s_flag[nb] - 1;
-      cbase[nb + 1] = cbase[nb] + cnt[nb];
-    }
+#pragma unroll
+    for (int nb = 0; nb < kNumNb; nb++) cbase[nb + 1] = cbase[nb] + (s_flag[nb] - 1);
     // Region offsets (constant divisors once the loop is unrolled).
     int roff[kNumNb];
     roff[0] = 0;

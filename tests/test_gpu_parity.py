@@ -282,3 +282,23 @@ def test_batch_merge_kernels_give_identical_results(mlpgpu_mod):
         p, x, y, t = cases[j]
         ot, ost = oracle.dvnd(t, oracle.dist(x, y, True), max_iters=limit)
         assert np.array_equal(out[2][j][0], ot) and out[2][j][1]["cost"] == ost["cost"], j
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_batch_tiny_and_mixed_sizes_with_int64_costs(mlpgpu_mod, wide):
+    """Edge sizes in the batched path: the smallest tours (n = 5 .. 12) next to
+    larger ones, 32-bit and 64-bit costs, the one-CTA merge (20 jobs) --
+    every job equal to the oracle's DVND."""
+    sizes = [5, 6, 7, 8, 9, 10, 11, 12, 13, 17, 23, 31, 40, 55, 64, 90, 128, 150, 201, 260]
+    b = mlpgpu_mod.Batch(wide=wide)
+    cases = []
+    for q, n in enumerate(sizes):
+        x, y = oracle.uniform_instance(n, 1300 + q)
+        t = oracle.random_perm_tour(n, 1300 + q)
+        b.add(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True), t)
+        cases.append((oracle.dist(x, y, True), t))
+    b.run()
+    for j, (D, t) in enumerate(cases):
+        bt, bst = b.result(j)
+        ot, ost = oracle.dvnd(t, D, wide=wide)
+        assert np.array_equal(bt, ot) and bst["cost"] == ost["cost"] and bst["moves"] == ost["moves"], sizes[j]

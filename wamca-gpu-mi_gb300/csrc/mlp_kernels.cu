@@ -323,10 +323,14 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   int c2A = -1, c2B = -1, cF[3] = {-1, -1, -1}, cB[3] = {-1, -1, -1};
   // E(x, y) around the pair (r, c) of row a; the four that row a + 1 shares
   // with row a are carried in registers.
-  C sM1P1 = (C)sS[0][b + 1];  // E(r-1, c)
-  C s0M1 = (C)sS[1][b - 1];   // E(r, c-1)
-  C s0P1 = (C)sS[1][b + 1];   // E(r, c+1)
-  C sP1P1 = (C)sS[2][b + 1];  // E(r+1, c+2)
+  int32_t sM1P1 = sS[0][b + 1];  // E(r-1, c)
+  int32_t s0M1 = sS[1][b - 1];   // E(r, c-1)
+  int32_t s0P1 = sS[1][b + 1];   // E(r, c+1)
+  int32_t sP1P1 = sS[2][b + 1];  // E(r+1, c+2)
+  // 64-bit costs: every factor of every product fits 32 bits (distances and
+  // weights <= 65535, positions < 16384, W <= 16392 * 65535 < 2^31), so each
+  // product is one exact widening multiply(-add) instead of a 64 x 64 one.
+  auto mw = [](int32_t x, int32_t y) -> int64_t { return (int64_t)x * (int64_t)y; };
 #pragma unroll 1
   for (int a = 1; a <= TR; a++) {
     const int r = r0 + a - 1;
@@ -334,20 +338,24 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
     const int c = r + L;
     const bool vpair = c <= sz - 2;
     const int qr = a - 1, qc = a + tid;
-    const C sP1M1 = (C)sS[a + 1][b - 1];  // E(r+1, c)
-    const C s00 = (C)sS[a][b];            // E(r, c)
-    const C s0P2 = (C)sS[a][b + 2];       // E(r, c+2)
-    const C sP2P1 = (C)sS[a + 2][b + 1];  // E(r+2, c+3)
-    const C wr0 = (C)sRw[qr], wr1 = (C)sRw[qr + 1];
-    const C wc0 = (C)sCw[qc], wc1 = (C)sCw[qc + 1];
-    const C Wr0 = sRW[qr], Wc0 = sCW[qc];
-    const C szr = (C)(sz - r), szc = (C)(sz - c);
+    const int32_t sP1M1 = sS[a + 1][b - 1];  // E(r+1, c)
+    const int32_t s00 = sS[a][b];            // E(r, c)
+    const int32_t s0P2 = sS[a][b + 2];       // E(r, c+2)
+    const int32_t sP2P1 = sS[a + 2][b + 1];  // E(r+2, c+3)
+    const int32_t wr0 = sRw[qr], wr1 = sRw[qr + 1];
+    const int32_t wc0 = sCw[qc], wc1 = sCw[qc + 1];
+    const int iszr = sz - r, iszc = sz - c;
+    const C szr = (C)iszr, szc = (C)iszc;
 
     // ---- swap (row-owned blocks): warp argmin per row ----
     if (mSw) {
       const bool v = vpair && L >= 2;
-      const V d = (V)(szr * (sM1P1 - wr0) + (szr - C(1)) * (sP1M1 - wr1) + szc * (s0M1 - wc0) +
-                      (szc - C(1)) * (s0P1 - wc1));
+      V d;
+      if constexpr (WIDE)
+        d = mw(iszr, sM1P1 - wr0) + mw(iszr - 1, sP1M1 - wr1) + mw(iszc, s0M1 - wc0) + mw(iszc - 1, s0P1 - wc1);
+      else
+        d = (V)(szr * ((C)sM1P1 - (C)wr0) + (szr - C(1)) * ((C)sP1M1 - (C)wr1) + szc * ((C)s0M1 - (C)wc0) +
+                (szc - C(1)) * ((C)s0P1 - (C)wc1));
       const int blkA = r - 1, blkB = sz - 3 - r;
       const bool hasA = blkA < nbS, hasB = blkB >= 0 && blkB < nbS;
       unsigned ties;
@@ -378,8 +386,13 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
 
     // ---- 2-opt (diagonal-owned blocks) ----
     if (m2o && vpair) {
-      const V d = (V)(szr * (sM1P1 - wr0) + (szc - C(1)) * (s0P1 - wc1) +
-                      C(2) * (sCQ[qc] - sRQ[qr]) - (C)(r + c + 1) * (Wc0 - Wr0));
+      V d;
+      if constexpr (WIDE)
+        d = mw(iszr, sM1P1 - wr0) + mw(iszc - 1, s0P1 - wc1) + 2 * ((int64_t)sCQ[qc] - (int64_t)sRQ[qr]) -
+            mw(r + c + 1, (int32_t)sCW[qc] - (int32_t)sRW[qr]);
+      else
+        d = (V)(szr * ((C)sM1P1 - (C)wr0) + (szc - C(1)) * ((C)s0P1 - (C)wc1) + C(2) * (sCQ[qc] - sRQ[qr]) -
+                (C)(r + c + 1) * (sCW[qc] - sRW[qr]));
       if (has2A && d < b2A) {
         b2A = d;
         c2A = c;
@@ -394,22 +407,37 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
 #pragma unroll
     for (int k = 1; k <= 3; k++) {
       if (!((mask >> (k + 1)) & 1) || c + k > sz - 1) continue;
-      const C Sf = k == 1 ? s0P1 : (k == 2 ? sP1P1 : sP2P1);  // E(r+k-1, c+k)
-      const C Sg = k == 1 ? s00 : (k == 2 ? s0P1 : s0P2);     // E(r, c+k-1)
-      const C wrk = (C)sRw[qr + k], wck = (C)sCw[qc + k];
-      const C kk = (C)k;
+      const int32_t Sf = k == 1 ? s0P1 : (k == 2 ? sP1P1 : sP2P1);  // E(r+k-1, c+k)
+      const int32_t Sg = k == 1 ? s00 : (k == 2 ? s0P1 : s0P2);     // E(r, c+k-1)
+      const int32_t wrk = sRw[qr + k], wck = sCw[qc + k];
       {
-        const V d = (V)(szr * ((C)sRA[k - 1][qr] - wr0) + (szc - kk) * (Sf - wck) + szc * Sg -
-                        (szr - kk) * wrk + ((C)r - (C)c) * (sRW[qr + k - 1] - Wr0) +
-                        kk * (sCW[qc + k - 1] - sRW[qr + k]));
+        V d;
+        if constexpr (WIDE) {
+          const int32_t Wr0 = (int32_t)sRW[qr];
+          d = mw(iszr, sRA[k - 1][qr] - wr0) + mw(iszc - k, Sf - wck) + mw(iszc, Sg) - mw(iszr - k, wrk) +
+              mw(r - c, (int32_t)sRW[qr + k - 1] - Wr0) + mw(k, (int32_t)sCW[qc + k - 1] - (int32_t)sRW[qr + k]);
+        } else {
+          const C kk = (C)k;
+          d = (V)(szr * ((C)sRA[k - 1][qr] - (C)wr0) + (szc - kk) * ((C)Sf - (C)wck) + szc * (C)Sg -
+                  (szr - kk) * (C)wrk + ((C)r - (C)c) * (sRW[qr + k - 1] - sRW[qr]) +
+                  kk * (sCW[qc + k - 1] - sRW[qr + k]));
+        }
         if (d < bF[k - 1]) {
           bF[k - 1] = d;
           cF[k - 1] = c;
         }
       }
       if (L >= 2) {
-        const V d = (V)(szr * (sM1P1 - wr0) + (szc - kk) * ((C)sCA[k - 1][qc] - wck) + (szr - kk) * Sg -
-                        szc * wc0 + (C)(c - r) * (sCW[qc + k - 1] - Wc0) - kk * (sCW[qc - 1] - Wr0));
+        V d;
+        if constexpr (WIDE) {
+          const int32_t Wc0 = (int32_t)sCW[qc];
+          d = mw(iszr, sM1P1 - wr0) + mw(iszc - k, sCA[k - 1][qc] - wck) + mw(iszr - k, Sg) - mw(iszc, wc0) +
+              mw(c - r, (int32_t)sCW[qc + k - 1] - Wc0) - mw(k, (int32_t)sCW[qc - 1] - (int32_t)sRW[qr]);
+        } else {
+          const C kk = (C)k;
+          d = (V)(szr * ((C)sM1P1 - (C)wr0) + (szc - kk) * ((C)sCA[k - 1][qc] - (C)wck) + (szr - kk) * (C)Sg -
+                  szc * (C)wc0 + (C)(c - r) * (sCW[qc + k - 1] - sCW[qc]) - kk * (sCW[qc - 1] - sRW[qr]));
+        }
         if (d <= bB[k - 1] && d != kInf) {
           bB[k - 1] = d;
           cB[k - 1] = c;

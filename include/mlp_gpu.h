@@ -122,6 +122,12 @@ MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len
 /* Same with the tour already in device memory (enqueued, no host sync). */
 MLP_API int mlp_solver_set_tour_device(mlp_solver_t s, const int32_t* tour_dev, int32_t len);
 MLP_API int mlp_solver_get_tour(mlp_solver_t s, int32_t* tour, int32_t len);
+/* Checkpoint / resume in the text format of MLSolution::save / load
+ * (source/mlsolution.cpp:685-751): tour length, cost, the tour.  Loading
+ * accepts a stored length of size or size - 1 as the reference does, reads
+ * size entries, validates the tour and recomputes the cost and ADS. */
+MLP_API int mlp_solver_save(mlp_solver_t s, const char* path);
+MLP_API int mlp_solver_load(mlp_solver_t s, const char* path);
 /* Device pointer to the solver's current tour (valid until destroy). */
 MLP_API int mlp_solver_tour_device(mlp_solver_t s, int32_t** tour_dev);
 /* Latency cost of the current tour (MLSolution::costCalc after update). */

@@ -302,3 +302,38 @@ def test_batch_tiny_and_mixed_sizes_with_int64_costs(mlpgpu_mod, wide):
         bt, bst = b.result(j)
         ot, ost = oracle.dvnd(t, D, wide=wide)
         assert np.array_equal(bt, ot) and bst["cost"] == ost["cost"] and bst["moves"] == ost["moves"], sizes[j]
+
+
+def test_checkpoint_resume_continues_the_same_search(mlpgpu_mod, tmp_path):
+    """A DVND stopped after some sweeps, saved in MLSolution's text format and
+    resumed in a new solver ends where the uninterrupted search ends."""
+    n = 400
+    x, y = oracle.uniform_instance(n, 88)
+    p = mlpgpu_mod.Problem.from_coords(x, y, dist_round=True)
+    t = oracle.random_perm_tour(n, 88)
+    full = mlpgpu_mod.Solver(p)
+    full.set_tour(t)
+    st_full = full.dvnd()
+    a = mlpgpu_mod.Solver(p)
+    a.set_tour(t)
+    st_a = a.dvnd(max_iters=20)
+    path = str(tmp_path / "ck.txt")
+    a.save(path)
+    tour_saved, cost_saved = mlpgpu_mod.load_solution(path)
+    assert np.array_equal(tour_saved, a.tour()) and cost_saved == st_a["cost"]
+    b = mlpgpu_mod.Solver(p)
+    b.load(path)
+    assert b.cost() == st_a["cost"]
+    st_b = b.dvnd()
+    assert np.array_equal(b.tour(), full.tour()) and st_b["cost"] == st_full["cost"]
+    assert st_a["sweeps"] + st_b["sweeps"] == st_full["sweeps"]
+    # A length written without the trailing depot (size - 1) is accepted, as
+    # the reference's loader does; the tour read is still size entries long.
+    bad = tmp_path / "short.txt"
+    bad.write_text(f"{n}\n0\n" + " ".join(str(v) for v in t) + "\n")
+    c = mlpgpu_mod.Solver(p)
+    c.load(str(bad))
+    assert np.array_equal(c.tour(), t)
+    (tmp_path / "trunc.txt").write_text(f"{n + 1}\n0\n0 1 2\n")
+    with pytest.raises(mlpgpu_mod.MLPError):
+        c.load(str(tmp_path / "trunc.txt"))

@@ -162,3 +162,21 @@ def test_legacy_better_no_conflict_quirks():
     assert imp == sum(moves[s][3] for s in sel)
     # noConflict(2opt, 2opt) uses (move2.j > move1.i - 1): almost always true
     assert oracle.legacy_no_conflict((1, 5, 9), (1, 6, 8))
+
+
+def test_solution_checkpoint_text_format(tmp_path, berlin):
+    """save_solution / load_solution use the text format of the reference's
+    MLSolution::save (tour length, cost, tour on one line)."""
+    import mlpgpu
+
+    t = np.array(berlin["random_tour_seed0"], np.int32)
+    p = tmp_path / "sol.txt"
+    cost = berlin["cost_random_tour_seed0"]
+    mlpgpu.save_solution(str(p), t, cost)
+    text = p.read_text()
+    assert text == f"{len(t)}\n{cost}\n" + " ".join(str(v) for v in t) + "\n"
+    t2, c2 = mlpgpu.load_solution(str(p))
+    assert np.array_equal(t2, t) and c2 == cost
+    (tmp_path / "bad.txt").write_text("53\n1\n0 1 2\n")
+    with pytest.raises(ValueError):
+        mlpgpu.load_solution(str(tmp_path / "bad.txt"))

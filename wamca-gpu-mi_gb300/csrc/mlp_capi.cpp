@@ -2,7 +2,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <memory>
 #include <vector>
 
@@ -249,6 +251,62 @@ MLP_API int mlp_solver_get_tour(mlp_solver_t s, int32_t* tour, int32_t len) {
            "copy tour");
   MLP_CUDA(cudaStreamSynchronize(s->set->stream()), "sync");
   return kOk;
+}
+
+// Checkpoint text format of MLSolution::save / load (source/mlsolution.cpp:685-751):
+// the tour length, the cost, then the tour on one line.
+MLP_API int mlp_solver_save(mlp_solver_t s, const char* path) {
+  if (!s || !path) return arg_error("null argument");
+  std::vector<int32_t> t(s->prob->size);
+  MLP_TRY(mlp_solver_get_tour(s, t.data(), (int32_t)t.size()));
+  int64_t cost = 0;
+  MLP_TRY(mlp_solver_cost(s, &cost));
+  FILE* f = std::fopen(path, "w");
+  if (!f) {
+    set_error(std::string("cannot write solution file: ") + path);
+    return kErrIo;
+  }
+  std::fprintf(f, "%d\n%lld\n", (int)t.size(), (long long)cost);
+  for (size_t q = 0; q < t.size(); q++) std::fprintf(f, q + 1 < t.size() ? "%d " : "%d\n", t[q]);
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) {
+    set_error(std::string("error writing solution file: ") + path);
+    return kErrIo;
+  }
+  return kOk;
+}
+
+MLP_API int mlp_solver_load(mlp_solver_t s, const char* path) {
+  if (!s || !path) return arg_error("null argument");
+  FILE* f = std::fopen(path, "r");
+  if (!f) {
+    set_error(std::string("cannot open solution file: ") + path);
+    return kErrIo;
+  }
+  const int size = s->prob->size;
+  long long v = 0, cost = 0;
+  std::vector<int32_t> t(size);
+  bool ok = std::fscanf(f, "%lld", &v) == 1;
+  // Like MLSolution::load: the stored length may be size or size - 1 (a file
+  // written for the other costTour setting); size entries follow the cost,
+  // which is recomputed rather than trusted.
+  if (ok && v != size && v != size - 1) {
+    std::fclose(f);
+    set_error("invalid solution file: tour length does not match the problem");
+    return kErrFormat;
+  }
+  ok = ok && std::fscanf(f, "%lld", &cost) == 1;
+  for (int q = 0; ok && q < size; q++) {
+    long long x = 0;
+    ok = std::fscanf(f, "%lld", &x) == 1 && x >= 0 && x < 65536;
+    t[q] = (int32_t)x;
+  }
+  std::fclose(f);
+  if (!ok) {
+    set_error("invalid solution file: truncated or malformed");
+    return kErrFormat;
+  }
+  return mlp_solver_set_tour(s, t.data(), size);
 }
 
 MLP_API int mlp_solver_tour_device(mlp_solver_t s, int32_t** tour) {

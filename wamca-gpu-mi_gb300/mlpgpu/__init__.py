@@ -98,6 +98,8 @@ def lib() -> C.CDLL:
         "mlp_solver_set_tour": (C.c_int, [vp, vp, i32]),
         "mlp_solver_set_tour_device": (C.c_int, [vp, vp, i32]),
         "mlp_solver_get_tour": (C.c_int, [vp, vp, i32]),
+        "mlp_solver_save": (C.c_int, [vp, C.c_char_p]),
+        "mlp_solver_load": (C.c_int, [vp, C.c_char_p]),
         "mlp_solver_tour_device": (C.c_int, [vp, P(vp)]),
         "mlp_solver_cost": (C.c_int, [vp, P(i64)]),
         "mlp_solver_weights": (C.c_int, [vp, vp, i32]),
@@ -287,6 +289,14 @@ class Solver:
     def set_tour_device(self, ptr: int) -> None:
         _check(lib().mlp_solver_set_tour_device(self._h, C.c_void_p(ptr), self.size))
 
+    def save(self, path: str) -> None:
+        """Writes the current tour and cost in MLSolution's text format."""
+        _check(lib().mlp_solver_save(self._h, path.encode()))
+
+    def load(self, path: str) -> None:
+        """Resumes from a tour saved in MLSolution's text format (cost recomputed)."""
+        _check(lib().mlp_solver_load(self._h, path.encode()))
+
     def tour(self) -> np.ndarray:
         t = np.zeros(self.size, np.int32)
         _check(lib().mlp_solver_get_tour(self._h, _ptr(t), self.size))
@@ -432,6 +442,28 @@ class Batch:
         st = DvndStats()
         _check(lib().mlp_batch_result(self._h, job, _ptr(t), len(t), C.byref(st)))
         return t, st.as_dict()
+
+
+def save_solution(path: str, tour: Sequence[int], cost: int) -> None:
+    """Checkpoints a result (e.g. of a served or batched search) in the text
+    format of the reference's MLSolution::save: tour length, cost, tour."""
+    t = [int(v) for v in tour]
+    with open(path, "w") as f:
+        f.write(f"{len(t)}\n{int(cost)}\n{' '.join(str(v) for v in t)}\n")
+
+
+def load_solution(path: str):
+    """Reads a tour saved by save_solution / mlp_solver_save / MLSolution::save;
+    returns (tour, stored cost).  Re-submit the tour to resume the search."""
+    with open(path) as f:
+        vals = f.read().split()
+    if len(vals) < 2:
+        raise ValueError("invalid solution file: missing length or cost")
+    size, cost = int(vals[0]), int(vals[1])
+    tour = np.array([int(v) for v in vals[2:2 + size]], dtype=np.int32)
+    if len(tour) != size:
+        raise ValueError("invalid solution file: truncated tour")
+    return tour, cost
 
 
 class Server:

@@ -116,6 +116,17 @@ MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
  * of mlp_solver_dvnd_async). */
 MLP_API int mlp_solver_set_tile_shape(mlp_solver_t s, int32_t shape);
 MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t iterations);
+/* Candidate mode of every later pass / DVND of this solver.  0 (default): one
+ * candidate per reference block (the ODC kernels).  1: TOTAL multi-improvement
+ * (the reference's isTotal kernels, source/mlkernel.h:150-163,
+ * mlkswap.cu:334-526, mlk2opt.cu:270-447, mlkoropt.cu:368-612, merged by
+ * mlkernel.cu:183-250): every move the neighbourhood evaluates is a candidate;
+ * per neighbourhood the improving ones are taken greedily in (delta, i, j)
+ * order, skipping any that conflicts with one taken before; a DVND iteration
+ * then merges the neighbourhoods' selections as usual.  The first switch to 1
+ * allocates the TOTAL lists: about 32 * size^2 bytes (64 * size^2 with 64-bit
+ * costs). */
+MLP_API int mlp_solver_set_total(mlp_solver_t s, int32_t on);
 /* Tour of `len` = size entries: tour[0] = tour[size-1] = 0 and a permutation of
  * 1..n-1 in between.  Rebuilds the ADS (update() + ldsUpdate()). */
 MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len);
@@ -221,6 +232,8 @@ MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape);
  * 16 jobs or more, otherwise a six-CTA cluster per job), 1 = cluster, 2 = one
  * CTA per job.  Every mode gives the same results. */
 MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode);
+/* Candidate mode of the batch's searches (as mlp_solver_set_total). */
+MLP_API int mlp_batch_set_total(mlp_batch_t b, int32_t on);
 /* Iterations between the host's convergence checks (default 16); after each
  * check the jobs that converged leave the launches. */
 MLP_API int mlp_batch_set_check_interval(mlp_batch_t b, int32_t iterations);

@@ -733,6 +733,154 @@ int orc_dvnd(int size, int32_t* tour, int n, const int32_t* D, int wide, int nb_
   return it;
 }
 
+}  // extern "C"
+
+/* ------------------------------------------------------------------------ */
+/* TOTAL multi-improvement                                                  */
+/* ------------------------------------------------------------------------ */
+namespace {
+
+// The TOTAL kernels (kernelSwapTotal mlkswap.cu:334-526, kernel2OptTotal
+// mlk2opt.cu:270-447, kernelOrOptTotal mlkoropt.cu:368-612) write one
+// candidate per thread instead of one per block (moveElems = grid.y *
+// block.x, mlkswap.cu:1022, mlkoropt.cu:851).  mergeGPU sorts them
+// (mlkernel.cu:256) and testSwapTotal / test2OptTotal / testOrOptTotal
+// (mlkernel.cu:183-250) zero every later move that conflicts with an earlier
+// negative one: the greedy independent set in sorted order, which the host
+// then applies in that order (WamcaExperiment.hpp:422-542).
+// Decisions: a thread evaluates one move (blockDim >= size), so every
+// distinct move (i, j) of the neighbourhood -- the moves of the ODC kernels'
+// mapping, each once -- is a candidate; ties are sorted by (i, j).
+struct TMove {
+  int64_t cost;
+  int32_t i, j;
+};
+
+void total_candidates(int nb, const Tour& T, const std::vector<int64_t>& w, const Prefix& P, int wide,
+                      std::vector<TMove>& out, int64_t* evals) {
+  const int size = T.size, m = num_blocks(nb, size), nthr = num_threads(nb, size);
+  std::vector<uint8_t> seen((size_t)size * size, 0);
+  out.clear();
+  int64_t ev = 0;
+  for (int by = 0; by < m; by++)
+    for (int ctx = 0; ctx < nthr; ctx++) {
+      int i, j;
+      map_move(nb, size, by, ctx, i, j);
+      ev++;  // evaluations counted as the kernels' threads (duplicates included)
+      uint8_t& s = seen[(size_t)i * size + j];
+      if (s) continue;
+      s = 1;
+      int64_t c;
+      if (nb == 0)
+        c = delta_swap(T, w, i, j);
+      else if (nb == 1)
+        c = fast_2opt(T, w, P, i, j);
+      else
+        c = fast_oropt(T, w, P, nb - 1, i, j);
+      c = wrap(c, wide);
+      if (c < 0) out.push_back(TMove{c, i, j});
+    }
+  std::sort(out.begin(), out.end(), [](const TMove& a, const TMove& b) {
+    if (a.cost != b.cost) return a.cost < b.cost;
+    if (a.i != b.i) return a.i < b.i;
+    return a.j < b.j;
+  });
+  if (evals) *evals += ev;
+}
+
+// testSwapTotal / test2OptTotal / testOrOptTotal, mlkernel.cu:183-250
+void total_select(int nb, const std::vector<TMove>& cands, std::vector<TMove>& kept) {
+  kept.clear();
+  const int id = move_id_of(nb);
+  for (const TMove& x : cands) {
+    bool ok = true;
+    for (const TMove& y : kept)
+      if (!can_same(nb, id, y.i, y.j, id, x.i, x.j)) {
+        ok = false;
+        break;
+      }
+    if (ok) kept.push_back(x);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_total_select(int nb, int size, const int32_t* tour, int n, const int32_t* D, int wide, int cap,
+                     int64_t* cost, int32_t* is, int32_t* js, int64_t* candidates) {
+  Tour T{size, tour, n, D};
+  std::vector<int64_t> w;
+  weights_of(T, w);
+  Prefix P;
+  P.build(w, size);
+  std::vector<TMove> cands, kept;
+  total_candidates(nb, T, w, P, wide, cands, nullptr);
+  total_select(nb, cands, kept);
+  for (size_t q = 0; q < kept.size() && (int)q < cap; q++) {
+    cost[q] = kept[q].cost;
+    is[q] = kept[q].i;
+    js[q] = kept[q].j;
+  }
+  if (candidates) *candidates = (int64_t)cands.size();
+  return (int)kept.size();
+}
+
+int orc_total_pass(int nb, int size, int32_t* tour, int n, const int32_t* D, int wide, int max_moves,
+                   int32_t* ids, int32_t* is, int32_t* js, int64_t* costs, int64_t* new_cost) {
+  std::vector<int64_t> c(size * 2 + 8);
+  std::vector<int32_t> ki(c.size()), kj(c.size());
+  const int k = orc_total_select(nb, size, tour, n, D, wide, (int)c.size(), c.data(), ki.data(), kj.data(),
+                                 nullptr);
+  for (int q = 0; q < k; q++) {
+    apply_move(move_id_of(nb), ki[q], kj[q], size, tour);
+    if (q < max_moves) {
+      ids[q] = move_id_of(nb);
+      is[q] = ki[q];
+      js[q] = kj[q];
+      costs[q] = c[q];
+    }
+  }
+  if (new_cost) *new_cost = cost_of(size, tour, n, D, wide, nullptr);
+  return k;
+}
+
+// DVND with TOTAL candidate sets: per iteration the TOTAL greedy of every
+// neighbourhood of `nbs` (ascending) on the same tour, then the cross-
+// neighbourhood greedy with canMerge (mlkernel.cu:649-864, stable on the
+// neighbourhood order and each neighbourhood's greedy order) and the apply.
+int orc_dvnd_total(int size, int32_t* tour, int n, const int32_t* D, int wide, int nb_count,
+                   const int32_t* nbs, int max_iters, int64_t* final_cost, int64_t* evals,
+                   int64_t* moves_applied) {
+  int it = 0;
+  int64_t ev = 0, mv = 0;
+  std::vector<int64_t> w;
+  Prefix P;
+  std::vector<TMove> cands, kept;
+  for (; it < max_iters; it++) {
+    Tour T{size, tour, n, D};
+    weights_of(T, w);
+    P.build(w, size);
+    std::vector<Cand> list;
+    for (int q = 0; q < nb_count; q++) {
+      const int nb = nbs[q];
+      total_candidates(nb, T, w, P, wide, cands, &ev);
+      total_select(nb, cands, kept);
+      for (size_t r = 0; r < kept.size(); r++)
+        list.push_back(Cand{kept[r].cost, nb, (int32_t)r, move_id_of(nb), kept[r].i, kept[r].j});
+    }
+    if (list.empty()) break;
+    std::vector<Cand> sel;
+    merge_cross(list, sel);
+    for (const Cand& x : sel) apply_move(x.id, x.i, x.j, size, tour);
+    mv += (int64_t)sel.size();
+  }
+  if (final_cost) *final_cost = cost_of(size, tour, n, D, wide, nullptr);
+  if (evals) *evals = ev;
+  if (moves_applied) *moves_applied = mv;
+  return it;
+}
+
 // noConflict, dvnd.cu:132-175 (including its typos; the MIN/MAX macros of
 // dvnd.cuh and the unsigned k of the Or-opt branches are reproduced).
 int orc_legacy_no_conflict(int id1, int i1, int j1, int id2, int i2, int j2) {

@@ -105,6 +105,20 @@ int orc_pass(int nb, int size, int32_t* tour, int n, const int32_t* D, int wide,
 int orc_dvnd(int size, int32_t* tour, int n, const int32_t* D, int wide,
              int nb_count, const int32_t* nbs, int max_iters, int threads,
              int64_t* final_cost, int64_t* evals, int64_t* moves_applied);
+/* ---- TOTAL multi-improvement (every evaluated move is a candidate) ---- */
+/* Kept moves of the TOTAL greedy of neighbourhood nb on `tour`, in greedy
+ * (delta, i, j) order: writes up to cap of them, returns their count;
+ * *candidates = number of improving moves it chose from. */
+int orc_total_select(int nb, int size, const int32_t* tour, int n, const int32_t* D, int wide,
+                     int cap, int64_t* cost, int32_t* is, int32_t* js, int64_t* candidates);
+/* One TOTAL pass of nb: select as above, apply in order, update. */
+int orc_total_pass(int nb, int size, int32_t* tour, int n, const int32_t* D, int wide,
+                   int max_moves, int32_t* ids, int32_t* is, int32_t* js, int64_t* costs,
+                   int64_t* new_cost);
+/* DVND whose iterations use TOTAL candidate sets (nbs ascending). */
+int orc_dvnd_total(int size, int32_t* tour, int n, const int32_t* D, int wide, int nb_count,
+                   const int32_t* nbs, int max_iters, int64_t* final_cost, int64_t* evals,
+                   int64_t* moves_applied);
 /* One full sweep of the given neighbourhoods (fast evaluator, OpenMP);
  * returns the number of move evaluations (for the CPU baseline). */
 int64_t orc_sweep(int size, const int32_t* tour, int n, const int32_t* D, int wide,

@@ -65,6 +65,9 @@ def lib() -> C.CDLL:
             "orc_pass": (i32, [i32, i32, vp, i32, vp, i32, i32, vp, vp, vp, vp, vp]),
             "orc_dvnd": (i32, [i32, vp, i32, vp, i32, i32, vp, i32, i32, vp, vp, vp]),
             "orc_sweep": (i64, [i32, vp, i32, vp, i32, i32, vp, i32, vp, vp, vp]),
+            "orc_total_select": (i32, [i32, i32, vp, i32, vp, i32, i32, vp, vp, vp, vp]),
+            "orc_total_pass": (i32, [i32, i32, vp, i32, vp, i32, i32, vp, vp, vp, vp, vp]),
+            "orc_dvnd_total": (i32, [i32, vp, i32, vp, i32, i32, vp, i32, vp, vp, vp]),
             "orc_legacy_no_conflict": (i32, [i32, i32, i32, i32, i32, i32]),
             "orc_legacy_better_no_conflict": (i32, [i32, vp, vp, vp, vp, vp, vp, i32, i32]),
             "orc_legacy_apply_moves": (C.c_uint32, [i32, vp, i32, vp, i32, vp, vp, vp]),
@@ -220,6 +223,42 @@ def dvnd(tour, D, wide: bool = False, nbs: Sequence[int] = range(5), max_iters: 
     fc, ev, mv = C.c_int64(), C.c_int64(), C.c_int64()
     it = lib().orc_dvnd(len(t), _p(t), D.shape[0], _p(D), int(wide), len(nbs_a), _p(nbs_a), max_iters, threads,
                         C.byref(fc), C.byref(ev), C.byref(mv))
+    return t, {"cost": fc.value, "iterations": it, "evals": ev.value, "moves": mv.value}
+
+
+def total_select(nb: int, tour, D, wide: bool = False):
+    """Kept moves [(cost, i, j)] of the TOTAL greedy of nb, in greedy order,
+    and the number of improving candidates."""
+    t, D = _i32(tour), _i32(D)
+    cap = 2 * len(t) + 8
+    c = np.zeros(cap, np.int64)
+    i = np.zeros(cap, np.int32)
+    j = np.zeros(cap, np.int32)
+    nc = C.c_int64()
+    k = lib().orc_total_select(nb, len(t), _p(t), D.shape[0], _p(D), int(wide), cap, _p(c), _p(i), _p(j),
+                               C.byref(nc))
+    return list(zip(c[:k].tolist(), i[:k].tolist(), j[:k].tolist())), nc.value
+
+
+def total_pass(nb: int, tour, D, wide: bool = False, max_moves: int = 1 << 15):
+    t, D = _i32(tour).copy(), _i32(D)
+    ids = np.zeros(max_moves, np.int32)
+    i = np.zeros(max_moves, np.int32)
+    j = np.zeros(max_moves, np.int32)
+    c = np.zeros(max_moves, np.int64)
+    nc = C.c_int64()
+    k = lib().orc_total_pass(nb, len(t), _p(t), D.shape[0], _p(D), int(wide), max_moves, _p(ids), _p(i), _p(j),
+                             _p(c), C.byref(nc))
+    kk = min(k, max_moves)
+    return t, nc.value, list(zip(ids[:kk].tolist(), i[:kk].tolist(), j[:kk].tolist(), c[:kk].tolist()))
+
+
+def dvnd_total(tour, D, wide: bool = False, nbs: Sequence[int] = range(5), max_iters: int = 1 << 20):
+    t, D = _i32(tour).copy(), _i32(D)
+    nbs_a = _i32(sorted(nbs))
+    fc, ev, mv = C.c_int64(), C.c_int64(), C.c_int64()
+    it = lib().orc_dvnd_total(len(t), _p(t), D.shape[0], _p(D), int(wide), len(nbs_a), _p(nbs_a), max_iters,
+                              C.byref(fc), C.byref(ev), C.byref(mv))
     return t, {"cost": fc.value, "iterations": it, "evals": ev.value, "moves": mv.value}
 
 

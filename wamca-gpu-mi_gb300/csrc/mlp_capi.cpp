@@ -225,6 +225,11 @@ MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t u) {
   return s->set->set_unroll(u);
 }
 
+MLP_API int mlp_solver_set_total(mlp_solver_t s, int32_t on) {
+  if (!s) return arg_error("null solver");
+  return s->set->set_total(on != 0);
+}
+
 MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len) {
   if (!s) return arg_error("null solver");
   MLP_TRY(validate_tour(tour, len, s->prob->n, s->prob->size));
@@ -585,6 +590,13 @@ MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode) {
   return kOk;
 }
 
+MLP_API int mlp_batch_set_total(mlp_batch_t b, int32_t on) {
+  if (!b) return arg_error("null batch");
+  b->total = on != 0;
+  if (b->set) return b->set->set_total(b->total);
+  return kOk;
+}
+
 MLP_API int mlp_batch_add(mlp_batch_t b, mlp_problem_t h, const int32_t* tour, int32_t len, int32_t* job) {
   Problem* p = reinterpret_cast<Problem*>(h);
   if (!b || !p) return arg_error("null argument");
@@ -616,6 +628,7 @@ static int batch_build(mlp_batch* b) {
   MLP_TRY(b->set->set_merge_mode(b->merge_mode));
   MLP_TRY(b->set->set_unroll(b->check_interval));
   MLP_TRY(b->set->init());
+  MLP_TRY(b->set->set_total(b->total));
   return batch_upload(b);
 }
 

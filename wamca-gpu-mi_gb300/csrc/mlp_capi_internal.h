@@ -25,6 +25,7 @@ struct mlp_batch {
   int mask = 0x1f;
   int merge_mode = 0;
   int check_interval = 16;
+  bool total = false;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<mlp::Job>> jobs;

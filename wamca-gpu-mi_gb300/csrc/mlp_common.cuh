@@ -113,6 +113,49 @@ MLP_HD int move_source(int id, int i, int j, int p) {
   return p < j + k ? p - j + i : p - k;
 }
 
+// ---------------- TOTAL candidate keys ----------------
+// A move of a TOTAL list is one key ordered by (delta, i, j): the delta with
+// its sign bit flipped above 14-bit i and j.  int32 mode: 60 bits of a uint64;
+// wide mode: 92 bits of a 128-bit integer.
+constexpr int kTotalKeyShift = 28;
+MLP_HD uint64_t total_key32(int32_t d, int i, int j) {
+  return ((uint64_t)((uint32_t)d ^ 0x80000000u) << kTotalKeyShift) | ((uint64_t)i << 14) | (uint64_t)j;
+}
+MLP_HD int32_t total_key32_delta(uint64_t k) { return (int32_t)((uint32_t)(k >> kTotalKeyShift) ^ 0x80000000u); }
+#ifdef __CUDACC__
+typedef unsigned __int128 u128;
+MLP_HD u128 total_key64(int64_t d, int i, int j) {
+  return ((u128)((uint64_t)d ^ 0x8000000000000000ull) << kTotalKeyShift) | ((u128)i << 14) | (u128)j;
+}
+MLP_HD int64_t total_key64_delta(u128 k) {
+  return (int64_t)((uint64_t)(k >> kTotalKeyShift) ^ 0x8000000000000000ull);
+}
+#endif
+// Capacity of neighbourhood nb's TOTAL list: swap and 2-opt have at most one
+// move per position pair, Or-opt-k one per ordered pair.
+MLP_HD int64_t total_list_cap(int nb, int size) {
+  const int64_t pairs = (int64_t)size * (size - 1) / 2;
+  return (nb < 2 ? pairs : 2 * pairs) + 64;
+}
+MLP_HD int64_t total_list_off(int nb, int size) {
+  int64_t o = 0;
+  for (int q = 0; q < nb; q++) o += total_list_cap(q, size);
+  return o;
+}
+
+// Stage-2 output region of neighbourhood nb: kept moves are independent
+// sets, at most size/4 + 1 swaps, size/3 + 1 2-opt and size/(k+2) + 1
+// Or-opt-k moves.
+MLP_HD int region_cap(int nb, int size) {
+  const int div = nb == 0 ? 4 : nb == 1 ? 2 : nb == 2 ? 3 : nb == 3 ? 4 : 5;
+  return size / div + 2;
+}
+MLP_HD int region_off(int nb, int size) {
+  int o = 0;
+  for (int q = 0; q < nb; q++) o += region_cap(q, size);
+  return o;
+}
+
 // ---------------- merge predicates ----------------
 MLP_HD int iabs_(int v) { return v < 0 ? -v : v; }
 MLP_HD int imin_(int a, int b) { return a < b ? a : b; }
@@ -218,6 +261,14 @@ struct JobDev {
   int32_t size;
   int32_t nb_mask;    // neighbourhoods evaluated and merged
   int32_t flags;
+  // TOTAL candidate mode (all null otherwise): the sweep appends every
+  // improving move to its neighbourhood's list, the TOTAL greedy writes the
+  // kept moves of neighbourhood nb at region_off(nb, size) + rank.
+  void* tlist;        // list nb: total_list_cap(nb) keys at total_list_off(nb)
+  int32_t* tcount;    // kNumNb list lengths
+  int64_t* tkcost;    // kept moves: delta
+  uint32_t* tkij;     // kept moves: i | j << 16
+  int32_t* tkcount;   // kNumNb kept counts
 };
 
 enum : int {

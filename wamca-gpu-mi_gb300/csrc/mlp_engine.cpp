@@ -267,9 +267,33 @@ size_t job_bytes(int size, bool wide, int moves_cap) {
 }
 
 Job::~Job() {
+  if (total) cudaFree(total);
   if (!arena) return;
   if (async_alloc) cudaFreeAsync(arena, alloc_stream);
   else cudaFree(arena);
+}
+
+size_t job_total_bytes(int size, bool wide) {
+  const size_t kept = (size_t)region_off(kNumNb, size);
+  return al(4 * kNumNb) * 2 + al(8 * kept) + al(4 * kept) +
+         al((size_t)total_list_off(kNumNb, size) * (wide ? 16 : 8));
+}
+
+int job_enable_total(Job* j) {
+  if (j->total) return kOk;
+  const size_t bytes = job_total_bytes(j->size, j->wide);
+  MLP_CUDA(cudaMalloc(&j->total, bytes), "cudaMalloc(TOTAL lists)");
+  const size_t kept = (size_t)region_off(kNumNb, j->size);
+  char* c = static_cast<char*>(j->total);
+  JobDev& d = j->dev;
+  d.tcount = (int32_t*)c;  c += al(4 * kNumNb);
+  d.tkcount = (int32_t*)c;  c += al(4 * kNumNb);
+  d.tkcost = (int64_t*)c;  c += al(8 * kept);
+  d.tkij = (uint32_t*)c;  c += al(4 * kept);
+  d.tlist = c;
+  j->total_bytes = bytes;
+  MLP_CUDA(cudaMemset(j->total, 0, al(4 * kNumNb) * 2), "memset(TOTAL counters)");
+  return kOk;
 }
 
 static void job_layout(Job* j, Problem* p, bool wide, int moves_cap);
@@ -559,6 +583,10 @@ int JobSet::set_shape(int shape) {
     set_error("tile shape index out of range");
     return kErrArg;
   }
+  if (total_) {  // the collecting sweep has one shape; this one applies afterwards
+    shape_user_ = shape;
+    return kOk;
+  }
   shape_ = shape;
   return djobs_ ? build_tiles() : kOk;
 }
@@ -624,7 +652,39 @@ bool JobSet::solo_merge() const {
   return merge_mode_ == kMergeSolo || (merge_mode_ == kMergeAuto && (int)jobs_.size() >= kSoloMinJobs);
 }
 
+int JobSet::set_total(bool on) {
+  if (on == total_) return kOk;
+  {
+    int st = ensure_all_active();
+    if (st != kOk) return st;
+  }
+  if (on) {
+    for (Job* j : all_jobs_) {
+      int st = job_enable_total(j);
+      if (st != kOk) return st;
+    }
+    std::vector<JobDev> h(jobs_.size());
+    for (size_t q = 0; q < jobs_.size(); q++) h[q] = jobs_[q]->dev;
+    MLP_CUDA(cudaMemcpyAsync(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice, stream_),
+             "copy jobs");
+    MLP_CUDA(cudaStreamSynchronize(stream_), "copy jobs");
+    shape_user_ = shape_;
+    shape_ = kTotalShape;
+  } else {
+    shape_ = shape_user_;
+  }
+  total_ = on;
+  return build_tiles();  // also drops the captured graphs
+}
+
 int JobSet::launch_iteration() {
+  if (total_) {
+    const int nj = (int)jobs_.size();
+    MLP_CUDA(launch_sweep_collect(dtiles_, ntiles_, djobs_, wide_, stream_), "sweep kernel");
+    MLP_CUDA(launch_total_select(djobs_, nj, wide_, stream_), "TOTAL greedy kernel");
+    MLP_CUDA(launch_total_finish(djobs_, nj, wide_, solo_smem_, max_size_, stream_), "merge kernel");
+    return kOk;
+  }
   MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
   if (solo_merge())
     MLP_CUDA(launch_merge_solo(djobs_, (int)jobs_.size(), wide_, solo_smem_, max_size_, stream_), "merge kernel");
@@ -831,7 +891,10 @@ int JobSet::read_stats(std::vector<std::array<int64_t, kStatWords>>* out) {
   int64_t err = 0;
   for (auto& a : *out) err |= a[kStatError];
   if (err) {
-    set_error("device reported an internal error");
+    static const char* what[] = {"", "", "merge stage-2 hand-off timed out", "kept-move region overflow",
+                                 "TOTAL list overflow", "TOTAL selection invariant broken"};
+    set_error(std::string("device reported an internal error (code ") + std::to_string(err) + ": " +
+              (err >= 2 && err <= 5 ? what[err] : "unknown") + ")");
     return kErrState;
   }
   return kOk;

@@ -80,6 +80,8 @@ struct Job {
   int moves_cap = 0;
   cudaStream_t alloc_stream = nullptr;
   bool async_alloc = false;
+  void* total = nullptr;  // TOTAL lists (allocated when a job set first enters TOTAL mode)
+  size_t total_bytes = 0;
   ~Job();
 };
 
@@ -89,6 +91,11 @@ int job_create_async(Problem* p, bool wide, cudaMemPool_t pool, cudaStream_t str
 // Per-job sweep tiles of one tile shape (job index 0).
 void job_tiles(int size, int shape, std::vector<SweepTile>* out);
 size_t job_bytes(int size, bool wide, int moves_cap);
+// Device bytes of a job's TOTAL lists (every improving move of each
+// neighbourhood, the per-neighbourhood greedy output and counters).
+size_t job_total_bytes(int size, bool wide);
+// Allocates the TOTAL lists once and points the descriptor at them.
+int job_enable_total(Job* j);
 
 enum MergeMode : int { kMergeAuto = 0, kMergeCluster = 1, kMergeSolo = 2 };
 constexpr int kSoloMinJobs = 16;
@@ -150,6 +157,10 @@ class JobSet {
   // or more, a six-CTA cluster per job otherwise), kMergeCluster, kMergeSolo.
   int set_merge_mode(int mode);
   bool solo_merge() const;
+  // TOTAL candidate mode: every move the sweep evaluates is a merge
+  // candidate (the reference's isTotal kernels), not only each block's best.
+  int set_total(bool on);
+  bool total() const { return total_; }
 
  private:
   int build_tiles();
@@ -166,6 +177,8 @@ class JobSet {
   bool merge_smem_ = true;
   bool solo_smem_ = true;
   int merge_mode_ = 0;
+  bool total_ = false;
+  int shape_user_ = -1;  // tile shape to restore when TOTAL mode ends
   JobDev* djobs_ = nullptr;
   SweepTile* dtiles_ = nullptr;
   int ntiles_ = 0;

@@ -183,6 +183,7 @@ __device__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t*
 __device__ void cta_reset_keys(const JobDev* J) {
   const int tb = total_blocks(J->size);
   for (int q = threadIdx.x; q < tb; q += blockDim.x) J->keys[q] = kKeyNone;
+  if (J->tcount != nullptr && threadIdx.x < kNumNb) J->tcount[threadIdx.x] = 0;
 }
 
 template <bool WIDE>
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(1024) k_prepare(const JobDev* __restrict__ job
 //   fwd-k     by = L-1, ctx = c-2
 //   bwd-k     by = size-k-1-L, ctx = size-k-1-c
 // --------------------------------------------------------------------------
-template <bool WIDE, int TL, int TR>
+template <bool WIDE, int TL, int TR, bool COLLECT = false>
 __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tiles,
                                               const JobDev* __restrict__ jobs, int improve_only) {
   using Ar = Arith<WIDE>;
@@ -331,6 +332,23 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   // weights <= 65535, positions < 16384, W <= 16392 * 65535 < 2^31), so each
   // product is one exact widening multiply(-add) instead of a 64 x 64 one.
   auto mw = [](int32_t x, int32_t y) -> int64_t { return (int64_t)x * (int64_t)y; };
+  // TOTAL candidate mode: every improving move (i, j) of neighbourhood nb is
+  // appended to nb's list, one atomic per warp and neighbourhood (every lane
+  // of the warp calls this at the same point).
+  auto emit = [&](int nb, bool p, V d, int i, int j) {
+    const unsigned bal = __ballot_sync(kFull, p);
+    if (bal == 0) return;
+    const int leader = __ffs(bal) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&J->tcount[nb], __popc(bal));
+    base = __shfl_sync(kFull, base, leader);
+    if (!p) return;
+    const int64_t pos = (int64_t)base + __popc(bal & ((1u << lane) - 1u));
+    if (pos >= total_list_cap(nb, sz)) return;  // the TOTAL greedy reports the overflow
+    const int64_t at = total_list_off(nb, sz) + pos;
+    if constexpr (WIDE) ((u128*)J->tlist)[at] = total_key64((int64_t)d, i, j);
+    else ((uint64_t*)J->tlist)[at] = total_key32((int32_t)d, i, j);
+  };
 #pragma unroll 1
   for (int a = 1; a <= TR; a++) {
     const int r = r0 + a - 1;
@@ -356,6 +374,9 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
       else
         d = (V)(szr * ((C)sM1P1 - (C)wr0) + (szr - C(1)) * ((C)sP1M1 - (C)wr1) + szc * ((C)s0M1 - (C)wc0) +
                 (szc - C(1)) * ((C)s0P1 - (C)wc1));
+      if constexpr (COLLECT) {
+        emit(0, v && d < 0, d, r, c);
+      } else {
       const int blkA = r - 1, blkB = sz - 3 - r;
       const bool hasA = blkA < nbS, hasB = blkB >= 0 && blkB < nbS;
       unsigned ties;
@@ -382,10 +403,11 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
           atomicMin((unsigned long long*)&keys[off0 + blkB],
                     (unsigned long long)make_key((int64_t)d, (uint32_t)(sz - 2 - c), kCtxBits));
       }
+      }
     }
 
     // ---- 2-opt (diagonal-owned blocks) ----
-    if (m2o && vpair) {
+    if (m2o && (COLLECT || vpair)) {
       V d;
       if constexpr (WIDE)
         d = mw(iszr, sM1P1 - wr0) + mw(iszc - 1, s0P1 - wc1) + 2 * ((int64_t)sCQ[qc] - (int64_t)sRQ[qr]) -
@@ -393,7 +415,8 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
       else
         d = (V)(szr * ((C)sM1P1 - (C)wr0) + (szc - C(1)) * ((C)s0P1 - (C)wc1) + C(2) * (sCQ[qc] - sRQ[qr]) -
                 (C)(r + c + 1) * (sCW[qc] - sRW[qr]));
-      if (has2A && d < b2A) {
+      if constexpr (COLLECT) emit(1, vpair && d < 0, d, r, c);
+      else if (has2A && d < b2A) {
         b2A = d;
         c2A = c;
       }
@@ -406,7 +429,9 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
     // ---- Or-opt-k forward (i=r, j=c) and backward (i=c, j=r) ----
 #pragma unroll
     for (int k = 1; k <= 3; k++) {
-      if (!((mask >> (k + 1)) & 1) || c + k > sz - 1) continue;
+      if (!((mask >> (k + 1)) & 1)) continue;
+      const bool vk = c + k <= sz - 1;
+      if (!COLLECT && !vk) continue;
       const int32_t Sf = k == 1 ? s0P1 : (k == 2 ? sP1P1 : sP2P1);  // E(r+k-1, c+k)
       const int32_t Sg = k == 1 ? s00 : (k == 2 ? s0P1 : s0P2);     // E(r, c+k-1)
       const int32_t wrk = sRw[qr + k], wck = sCw[qc + k];
@@ -422,12 +447,14 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
                   (szr - kk) * (C)wrk + ((C)r - (C)c) * (sRW[qr + k - 1] - sRW[qr]) +
                   kk * (sCW[qc + k - 1] - sRW[qr + k]));
         }
-        if (d < bF[k - 1]) {
+        if constexpr (COLLECT) {
+          emit(k + 1, vk && d < 0, d, r, c);
+        } else if (d < bF[k - 1]) {
           bF[k - 1] = d;
           cF[k - 1] = c;
         }
       }
-      if (L >= 2) {
+      if (COLLECT || L >= 2) {
         V d;
         if constexpr (WIDE) {
           const int32_t Wc0 = (int32_t)sCW[qc];
@@ -438,7 +465,9 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
           d = (V)(szr * ((C)sM1P1 - (C)wr0) + (szc - kk) * ((C)sCA[k - 1][qc] - (C)wck) + (szr - kk) * (C)Sg -
                   szc * (C)wc0 + (C)(c - r) * (sCW[qc + k - 1] - sCW[qc]) - kk * (sCW[qc - 1] - sRW[qr]));
         }
-        if (d <= bB[k - 1] && d != kInf) {
+        if constexpr (COLLECT) {
+          emit(k + 1, vk && L >= 2 && d < 0, d, c, r);
+        } else if (d <= bB[k - 1] && d != kInf) {
           bB[k - 1] = d;
           cB[k - 1] = c;
         }
@@ -452,6 +481,7 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
 
   // DVND sweeps publish improving candidates only (the merge ignores the
   // rest); evaluation sweeps publish every block's best.
+  if constexpr (COLLECT) return;
 
   if (c2A >= 0 && (!improve_only || b2A < 0))
     atomicMin((unsigned long long*)&keys[off1 + (L - 1)],
@@ -492,15 +522,6 @@ constexpr int kClusterCtas = 6;  // five stage-2 CTAs and the stage-3 leader
 //      reused for the apply owner map once stage 3 has compacted the kept set
 //   B: swap endpoint tables (stage 2), then the stage-3 move list and bit rows
 //   T: the old and the new tour
-__host__ __device__ __forceinline__ int region_cap(int nb, int size) {
-  const int div = nb == 0 ? 4 : nb == 1 ? 2 : nb == 2 ? 3 : nb == 3 ? 4 : 5;
-  return size / div + 2;
-}
-__host__ __device__ __forceinline__ int region_off(int nb, int size) {
-  int o = 0;
-  for (int q = 0; q < nb; q++) o += region_cap(q, size);
-  return o;
-}
 
 struct MergeLayout {
   int tb, mmax, m3cap;
@@ -1128,6 +1149,54 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
 }
 
 // --------------------------------------------------------------------------
+// End of a TOTAL iteration: the moves kept by the TOTAL greedy of every
+// neighbourhood (k_total_select, mlp_total.cu) form the stage-3 list, keyed
+// (delta, neighbourhood, rank in that greedy's order); merge_finish then runs
+// the cross-neighbourhood greedy, the apply and the ADS rebuild as after
+// k_merge_solo.  One CTA per job.
+// --------------------------------------------------------------------------
+template <bool WIDE>
+__global__ void __launch_bounds__(kSoloThreads) k_total_finish(const JobDev* __restrict__ jobs, int use_smem) {
+  extern __shared__ __align__(16) uint8_t dsm[];
+  const JobDev* J = jobs + blockIdx.x;
+  {
+    const int64_t* stt = J->stats;
+    if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;
+  }
+  const int sz = J->size, mask = J->nb_mask, tid = threadIdx.x, nt = blockDim.x;
+  const SoloLayout lay(sz);
+  uint8_t* ws = use_smem ? dsm : J->ws;
+  uint64_t* key3 = (uint64_t*)(ws + lay.o_key3);
+  uint64_t* shp3 = (uint64_t*)(ws + lay.o_shp3);
+  uint32_t* ij3 = (uint32_t*)(ws + lay.o_ij3);
+  volatile uint8_t* st3 = (volatile uint8_t*)(ws + lay.o_st3);
+  int m3 = 0;
+  for (int nb = 0; nb < kNumNb; nb++) {
+    if (!((mask >> nb) & 1)) continue;
+    const int cnt = J->tkcount[nb], base = region_off(nb, sz);
+    for (int r = tid; r < cnt; r += nt) {
+      const int slot = m3 + r;
+      if (slot >= lay.m3cap) break;
+      const uint32_t ijx = J->tkij[base + r];
+      key3[slot] = make_key(J->tkcost[base + r], ((uint32_t)nb << kCtxBits) | (uint32_t)r, kCtxBits + 3);
+      shp3[slot] = move_shape(nb, (int)(ijx & 0xffff), (int)(ijx >> 16));
+      ij3[slot] = ijx;
+      st3[slot] = kUndec;
+    }
+    m3 += cnt;
+  }
+  if (m3 > lay.m3cap) {
+    if (tid == 0) J->stats[kStatError] = 3;
+    m3 = lay.m3cap;
+  }
+  int32_t* t_old = (int32_t*)(ws + lay.o_told);
+  for (int p = tid; p < sz; p += nt) t_old[p] = J->tour[p];
+  __syncthreads();
+  merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
+                     t_old, (int32_t*)(ws + lay.o_tnew));
+}
+
+// --------------------------------------------------------------------------
 // Reference ADS buffer (mlads.h:38-74, filled like MLSolution::ldsUpdate,
 // mlsolution.cpp:420-486).  C is written from the closed form
 //   C[i][j] = (P[j] - P[i]) - (j - i) T[i]          (i < j)
@@ -1269,6 +1338,12 @@ __global__ void k_loop_condition(const JobDev* __restrict__ jobs, int njobs, cud
 }
 
 template <bool WIDE, int TL, int TR>
+cudaError_t sweep_collect_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, cudaStream_t s) {
+  k_sweep<WIDE, TL, TR, true><<<ntiles, TL, 0, s>>>(tiles, jobs, 1);
+  return cudaGetLastError();
+}
+
+template <bool WIDE, int TL, int TR>
 cudaError_t sweep_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, int improve_only,
                          cudaStream_t s) {
   k_sweep<WIDE, TL, TR><<<ntiles, TL, 0, s>>>(tiles, jobs, improve_only);
@@ -1339,6 +1414,23 @@ cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs,
               : sweep_dispatch<false>(tiles, ntiles, jobs, shape, io, s);
 }
 
+cudaError_t launch_sweep_collect(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
+                                 cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  static_assert(kTileShapes[kTotalShape].tl == 32 && kTileShapes[kTotalShape].tr == 16, "collect tile shape");
+  return wide ? sweep_collect_launch<true, 32, 16>(tiles, ntiles, jobs, s)
+              : sweep_collect_launch<false, 32, 16>(tiles, ntiles, jobs, s);
+}
+
+cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
+                                cudaStream_t s) {
+  if (njobs <= 0) return cudaSuccess;
+  const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
+  if (wide) k_total_finish<true><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  else k_total_finish<false><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  return cudaGetLastError();
+}
+
 cudaError_t configure_prepare() {
   cudaError_t e = cudaFuncSetAttribute(k_prepare<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(sizeof(int32_t) * kMaxSize));
@@ -1365,7 +1457,13 @@ cudaError_t configure_merge(size_t bytes) {
   const int solo = (int)SoloLayout(solo_smem_max_size()).total;
   e = cudaFuncSetAttribute(k_merge_solo<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_merge_solo<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  e = cudaFuncSetAttribute(k_merge_solo<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_total_finish<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_total_finish<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  if (e != cudaSuccess) return e;
+  return configure_total();
 }
 
 cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,

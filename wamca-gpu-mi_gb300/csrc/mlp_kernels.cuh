@@ -56,6 +56,19 @@ cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem
 // One CTA per job (throughput: sets of many jobs).  Identical results.
 cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
                               cudaStream_t s);
+// TOTAL candidate mode (every evaluated move is a merge candidate).
+// The collecting sweep appends each job's improving moves to its TOTAL lists
+// (tile shape kTotalShape); the TOTAL greedy selects per neighbourhood
+// (mlp_total.cu); the finish runs the cross-neighbourhood greedy, apply and
+// ADS rebuild (one CTA per job, the k_merge_solo workspace).
+constexpr int kTotalShape = 2;  // 32 diagonals x 16 rows
+cudaError_t launch_sweep_collect(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
+                                 cudaStream_t s);
+cudaError_t launch_total_select(const JobDev* jobs, int njobs, bool wide, cudaStream_t s);
+cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
+                                cudaStream_t s);
+// Opt the TOTAL greedy into its dynamic shared memory (configure_merge calls it).
+cudaError_t configure_total();
 // Reference ADS buffer (source/mlads.h:38-74) of each job's current tour.
 cudaError_t launch_ads(const JobDev* job, const int32_t* cx, const int32_t* cy, uint32_t* ads,
                        int cost_tour, int dist_round, cudaStream_t s, uint32_t* Pbuf, int size);

@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
         "mlp_solver_set_stream": (C.c_int, [vp, vp]),
         "mlp_solver_set_tile_shape": (C.c_int, [vp, i32]),
         "mlp_solver_set_unroll": (C.c_int, [vp, i32]),
+        "mlp_solver_set_total": (C.c_int, [vp, i32]),
         "mlp_solver_set_tour": (C.c_int, [vp, vp, i32]),
         "mlp_solver_set_tour_device": (C.c_int, [vp, vp, i32]),
         "mlp_solver_get_tour": (C.c_int, [vp, vp, i32]),
@@ -124,6 +125,7 @@ def lib() -> C.CDLL:
         "mlp_batch_set_stream": (C.c_int, [vp, vp]),
         "mlp_batch_set_tile_shape": (C.c_int, [vp, i32]),
         "mlp_batch_set_merge_mode": (C.c_int, [vp, i32]),
+        "mlp_batch_set_total": (C.c_int, [vp, i32]),
         "mlp_batch_set_check_interval": (C.c_int, [vp, i32]),
         "mlp_batch_add": (C.c_int, [vp, vp, vp, i32, P(i32)]),
         "mlp_batch_run": (C.c_int, [vp, i32, i32]),
@@ -282,6 +284,11 @@ class Solver:
     def set_unroll(self, u: int) -> None:
         _check(lib().mlp_solver_set_unroll(self._h, u))
 
+    def set_total(self, on: bool = True) -> None:
+        """TOTAL multi-improvement (MLKernel isTotal): every evaluated move is a
+        merge candidate, not only each reference block's best."""
+        _check(lib().mlp_solver_set_total(self._h, int(bool(on))))
+
     def set_tour(self, tour: Sequence[int]) -> None:
         t = _i32(tour)
         _check(lib().mlp_solver_set_tour(self._h, _ptr(t), len(t)))
@@ -415,6 +422,10 @@ class Batch:
     def set_merge_mode(self, mode: int) -> None:
         """0 automatic, 1 six-CTA cluster per job, 2 one CTA per job."""
         _check(lib().mlp_batch_set_merge_mode(self._h, mode))
+
+    def set_total(self, on: bool = True) -> None:
+        """TOTAL candidate mode for every search of the batch (as Solver.set_total)."""
+        _check(lib().mlp_batch_set_total(self._h, int(bool(on))))
 
     def set_check_interval(self, iterations: int) -> None:
         """Iterations between convergence checks (converged jobs then leave the launches)."""

@@ -21,6 +21,9 @@ Beside the headline, in the same line:
              several offered rates: solves/s, p50/p99 latency, 40 GB budget
   large      n = 10000 with int64 costs: a 2-opt + Or-opt-3 sweep and a DVND
              capped in sweeps
+  total      TOTAL multi-improvement at n = 1000 (every evaluated move a merge
+             candidate): one pass per neighbourhood and a whole DVND, beside
+             the oracle's CPU time for the same work
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -536,6 +539,84 @@ def bench_large(args, mlpgpu, workloads, stream, flush):
                             "evals_per_s": st["evals"] / t_d, "cost": st["cost"], "converged": st["converged"]}}
 
 
+def bench_total(args, mlpgpu, workloads, stream, flush):
+    """TOTAL multi-improvement (every evaluated move is a merge candidate, the
+    reference's isTotal kernels) on the n = 1000 instance from a seeded random
+    start: one TOTAL pass per neighbourhood (collecting sweep + greedy over all
+    improving moves + apply) and a whole TOTAL DVND, each against the oracle's
+    CPU restatement on the same input."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU-baseline leg of this workload, and its checker
+
+    n = N_NODES
+    x, y = workloads.uniform_instance(n, INSTANCE_SEED)
+    t0 = workloads.random_perm_tour(n, 7)
+    prob = mlpgpu.Problem.from_coords(x, y, dist_round=True)
+    s = mlpgpu.Solver(prob, wide=False)
+    s.set_stream(stream.cuda_stream)
+    s.set_total(True)
+    D = oracle.dist(x, y, True)
+    passes = {}
+    for nb, name in enumerate(["swap", "2opt", "oropt1", "oropt2", "oropt3"]):
+        times, moves = [], None
+        for r in range(args.total_reps + 2):
+            s.set_tour(t0)
+            torch.cuda.synchronize()
+            a, b = _events(2)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                a.record(stream)
+                s.begin(1 << nb, 1)
+                s.enqueue(1)
+                b.record(stream)
+            torch.cuda.synchronize()
+            if r >= 2:
+                times.append(a.elapsed_time(b))
+            moves = s.stats()["moves"]
+        c0 = time.perf_counter()
+        kept, ncand = oracle.total_select(nb, t0, D)
+        oracle.total_pass(nb, t0, D)
+        cpu_s = (time.perf_counter() - c0) / 2
+        assert len(kept) == moves, "TOTAL pass disagrees with the oracle"
+        passes[name] = {"gpu_ms": statistics.median(times), "improving_candidates": ncand, "moves_applied": moves,
+                        "cpu_oracle_ms": cpu_s * 1e3}
+    s.set_tour(t0)
+    torch.cuda.synchronize()
+    a, b = _events(2)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        st = s.dvnd(mlpgpu.NB_ALL)
+        b.record(stream)
+    torch.cuda.synchronize()
+    t_d = a.elapsed_time(b) * 1e-3
+    c0 = time.perf_counter()
+    _, ost = oracle.dvnd_total(t0, D, max_iters=args.total_cpu_iters)
+    cpu_it = (time.perf_counter() - c0) / max(1, ost["iterations"])
+    s.set_total(False)
+    s.set_tour(t0)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        st2 = s.dvnd(mlpgpu.NB_ALL)
+        b.record(stream)
+    torch.cuda.synchronize()
+    t_p = a.elapsed_time(b) * 1e-3
+    return {"workload": f"n={n} uniform, one seeded random start; TOTAL pass per neighbourhood and a TOTAL DVND "
+                        "to a local optimum (device time, L2 flushed before each pass)",
+            "passes": passes,
+            "dvnd": {"seconds": t_d, "sweeps": st["sweeps"], "moves": st["moves"], "cost": st["cost"],
+                     "ms_per_iteration": 1e3 * t_d / st["sweeps"],
+                     "cpu_oracle_ms_per_iteration": cpu_it * 1e3,
+                     "cpu_oracle_sample": f"first {ost['iterations']} iterations, 1 thread"},
+            "per_block_dvnd_same_start": {"seconds": t_p, "sweeps": st2["sweeps"], "cost": st2["cost"]},
+            "reference_published": {"note": "reference logs, n=1000 TRP-S1000-R1, one TOTAL swap pass, unknown GPU "
+                                            "(CUDA 8), CPU clock around launch+sync",
+                                    "swap_kernel_ms": 2.311, "swap_gpu_merge_ms": 424.9,
+                                    "swap_cpu_graph_merge_ms": 17838.6}}
+
+
 def run_ours(args, world, rank, local) -> None:
     import torch
 
@@ -555,7 +636,8 @@ def run_ours(args, world, rank, local) -> None:
         # One workload alone (profiling runs); prints its object, not the bench line.
         fn = {"batched": lambda: bench_batched(args, mlpgpu, workloads, stream),
               "serving": lambda: bench_serving(args, mlpgpu, workloads),
-              "large": lambda: bench_large(args, mlpgpu, workloads, stream, flush)}[args.only]
+              "large": lambda: bench_large(args, mlpgpu, workloads, stream, flush),
+              "total": lambda: bench_total(args, mlpgpu, workloads, stream, flush)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}))
         return
@@ -576,6 +658,8 @@ def run_ours(args, world, rank, local) -> None:
             extra["serving"] = bench_serving(args, mlpgpu, workloads)
         if "large" in wl:
             extra["large"] = bench_large(args, mlpgpu, workloads, stream, flush)
+        if "total" in wl:
+            extra["total"] = bench_total(args, mlpgpu, workloads, stream, flush)
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -631,7 +715,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-iters", type=int, default=1 << 20)
-    ap.add_argument("--workloads", default="batched,serving,large",
+    ap.add_argument("--workloads", default="batched,serving,large,total",
                     help="extra workloads reported beside the plain n=1000 headline")
     ap.add_argument("--batch-instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=128)
@@ -641,7 +725,9 @@ def main() -> None:
     ap.add_argument("--serve-iters", type=int, default=2)
     ap.add_argument("--large-n", type=int, default=10000)
     ap.add_argument("--large-iters", type=int, default=300)
-    ap.add_argument("--only", choices=["batched", "serving", "large"], default=None,
+    ap.add_argument("--total-reps", type=int, default=5)
+    ap.add_argument("--total-cpu-iters", type=int, default=8)
+    ap.add_argument("--only", choices=["batched", "serving", "large", "total"], default=None,
                     help="run one extra workload alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

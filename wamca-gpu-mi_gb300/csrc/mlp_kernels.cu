@@ -1153,10 +1153,10 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
 // neighbourhood (k_total_select, mlp_total.cu) form the stage-3 list, keyed
 // (delta, neighbourhood, rank in that greedy's order); merge_finish then runs
 // the cross-neighbourhood greedy, the apply and the ADS rebuild as after
-// k_merge_solo.  One CTA per job.
+// k_merge_solo.  One 1024-thread CTA per job (the k_merge_solo workspace).
 // --------------------------------------------------------------------------
 template <bool WIDE>
-__global__ void __launch_bounds__(kSoloThreads) k_total_finish(const JobDev* __restrict__ jobs, int use_smem) {
+__global__ void __launch_bounds__(kMergeThreads) k_total_finish(const JobDev* __restrict__ jobs, int use_smem) {
   extern __shared__ __align__(16) uint8_t dsm[];
   const JobDev* J = jobs + blockIdx.x;
   {
@@ -1426,8 +1426,8 @@ cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool u
                                 cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
   const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
-  if (wide) k_total_finish<true><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
-  else k_total_finish<false><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  if (wide) k_total_finish<true><<<njobs, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  else k_total_finish<false><<<njobs, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -36,21 +36,25 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTotThreads = 1024;
-constexpr int kTotBatch = 512;     // keys resolved per batch
+constexpr int kTotBatch = 256;     // keys resolved per batch
 constexpr int kTotBins = 2048;     // histogram bins of the threshold search
 constexpr int kCovWords = kMaxSize / 32 + 4;
 enum : uint8_t { kNone = 0, kUndec = 1, kIn = 2, kOut = 3 };
 
+// Keys loaded per thread per step of a pass over a list: independent loads
+// in flight hide the L2 latency (a single CTA streams the whole list).
 template <bool WIDE>
 struct TK;
 template <>
 struct TK<false> {
   using K = uint64_t;
+  static constexpr int U = 8;
   static __device__ __forceinline__ int64_t delta(K k) { return total_key32_delta(k); }
 };
 template <>
 struct TK<true> {
   using K = u128;
+  static constexpr int U = 4;
   static __device__ __forceinline__ int64_t delta(K k) { return total_key64_delta(k); }
 };
 
@@ -118,15 +122,46 @@ __device__ int block_scan_int(int v, int* sm, int& total) {
   __syncthreads();  // sm may still be read by a previous call
   if (lane == 31) sm[wid] = x;
   __syncthreads();
-  int before = 0;
-  total = 0;
-  for (int w = 0; w < nw; w++) {
-    const int s = sm[w];
-    if (w < wid) before += s;
-    total += s;
+  int s = lane < nw ? sm[lane] : 0;  // every warp scans the warp totals
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, s, o);
+    if (lane >= o) s += y;
   }
+  total = __shfl_sync(kFull, s, 31);
+  const int before = wid > 0 ? __shfl_sync(kFull, s, wid - 1) : 0;
   return before + x - v;
 }
+
+// Exclusive scan of one value per warp (v equal on the warp's lanes).
+__device__ int block_scan_warps(int v, int* sm, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();  // sm may still be read by a previous call
+  if (lane == 0) sm[wid] = v;
+  __syncthreads();
+  int s = lane < nw ? sm[lane] : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, s, o);
+    if (lane >= o) s += y;
+  }
+  total = __shfl_sync(kFull, s, 31);
+  return wid > 0 ? __shfl_sync(kFull, s, wid - 1) : 0;
+}
+
+__device__ __forceinline__ void hist_add(uint32_t* hist, int bin) {
+  if (bin >= 0) atomicAdd(&hist[bin], 1u);
+}
+
+// Bin of key k in the histogram of [lo, lo + range] with bins of 2^sft
+// (-1 outside).
+template <typename K>
+__device__ __forceinline__ int bin_of(K k, K lo, K range, int sft) {
+  if (k < lo) return -1;
+  const K off = k - lo;
+  return off <= range ? (int)(uint32_t)(off >> sft) : -1;
+}
+__device__ __forceinline__ int bin_shift(int bl) { return bl > 11 ? bl - 11 : 0; }
 
 // The move (i, j) of a key, and its conflict footprint ab: swap endpoints
 // i | j << 16, else the closed conflict interval a | b << 16.
@@ -205,13 +240,27 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
   }
   const int kbase = region_off(nb, sz), kcap = region_cap(nb, sz);
   int nk = 0;
-  K kmin = kmax_value<K>(), kmax = 0;
-  for (int x = tid; x < m; x += nt) {
-    const K k = list[x];
-    kmin = k < kmin ? k : kmin;
-    kmax = k > kmax ? k : kmax;
+  K lo = kmax_value<K>(), hi = 0;
+  constexpr int U = TK<WIDE>::U;
+  for (int x0 = 0; x0 < m; x0 += U * nt) {
+    K kv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int x = x0 + u * nt + tid;
+      kv[u] = x < m ? list[x] : kmax_value<K>();
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int x = x0 + u * nt + tid;
+      if (x < m) {
+        lo = kv[u] < lo ? kv[u] : lo;
+        hi = kv[u] > hi ? kv[u] : hi;
+      }
+    }
   }
-  block_minmax(kmin, kmax, s_red);
+  block_minmax(lo, hi, s_red);
+  K range = hi - lo;
+  int sft = bin_shift(bitlen(range));
 
   for (int round = 0; m > 0; round++) {
     if (round > (1 << 24)) {  // unreachable: every round removes at least the smallest key
@@ -219,44 +268,69 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       break;
     }
     // ---- 1. threshold: at most kTotBatch keys <= T ----
-    K T = kmax;
+    // Every remaining key lies in [lo, hi]; histogram of [lo, lo + range] in
+    // bins of 2^sft.
+    K T = hi;
     if (m > kTotBatch) {
-      K range = kmax - kmin;
+      // Take the lowest bins that fit the budget; while less than half of
+      // the batch is filled, refine into the first bin that did not fit.
+      int budget = kTotBatch;
+      bool have_t = false;
       for (int lvl = 0; lvl < 16; lvl++) {
-        const int bl = bitlen(range);
-        const int sft = bl > 11 ? bl - 11 : 0;
         for (int q = tid; q < kTotBins; q += nt) hist[q] = 0;
         __syncthreads();
-        for (int x = tid; x < m; x += nt) {
-          const K off = list[x] - kmin;
-          if (off <= range) atomicAdd(&hist[(uint32_t)(off >> sft)], 1u);
+        for (int x0 = 0; x0 < m; x0 += U * nt) {
+          K kv[U];
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            const int x = x0 + u * nt + tid;
+            kv[u] = x < m ? list[x] : kmax_value<K>();
+          }
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            hist_add(hist, x0 + u * nt + tid < m ? bin_of(kv[u], lo, range, sft) : -1);
         }
         if (tid == 0) s_g = -1;
         __syncthreads();
         const int h0 = (int)hist[2 * tid], h1 = (int)hist[2 * tid + 1];
         int tot;
         const int e = block_scan_int(h0 + h1, s_scan, tot);
-        int g = -1;
-        if (e + h0 <= kTotBatch) g = 2 * tid;
-        if (e + h0 + h1 <= kTotBatch) g = 2 * tid + 1;
-        if (g >= 0) atomicMax(&s_g, g);
+        // (last bin that fits) << 20 | (keys up to it): both grow together
+        int packed = -1;
+        if (e + h0 <= budget) packed = ((2 * tid) << 20) | (e + h0);
+        if (e + h0 + h1 <= budget) packed = ((2 * tid + 1) << 20) | (e + h0 + h1);
+        if (packed >= 0) atomicMax(&s_g, packed);
         __syncthreads();
-        const int gg = s_g;
+        const int pk = s_g;
+        const int gg = pk >= 0 ? pk >> 20 : -1;
         if (gg >= 0) {
-          T = kmin + ((K)(gg + 1) << sft) - 1;
-          break;
+          T = lo + ((K)(gg + 1) << sft) - 1;
+          have_t = true;
+          budget -= pk & 0xfffff;
         }
-        range = ((K)1 << sft) - 1;  // sft > 0: keys are distinct, a one-key bin never overflows
+        if (gg == kTotBins - 1 || sft == 0 || budget < kTotBatch / 2) break;
+        lo = lo + ((K)(gg + 1) << sft);  // the first bin that did not fit
+        range = ((K)1 << sft) - 1;
+        sft = bin_shift(bitlen(range));
       }
+      if (!have_t) T = hi;  // unreachable: single-key bins always fit
     }
     // ---- 2. gather the keys <= T and sort them ----
     if (tid == 0) s_nbat = 0;
     __syncthreads();
-    for (int x = tid; x < m; x += nt) {
-      const K k = list[x];
-      if (k <= T) {
-        const int q = atomicAdd(&s_nbat, 1);
-        if (q < kTotBatch) bat[q] = k;
+    for (int x0 = 0; x0 < m; x0 += U * nt) {
+      K kv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int x = x0 + u * nt + tid;
+        kv[u] = x < m ? list[x] : kmax_value<K>();
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (x0 + u * nt + tid < m && kv[u] <= T) {
+          const int q = atomicAdd(&s_nbat, 1);
+          if (q < kTotBatch) bat[q] = kv[u];
+        }
       }
     }
     __syncthreads();
@@ -306,11 +380,20 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       // bit y of row x <=> y precedes x and the two conflict
       for (int x = wid; x < na; x += nw) {
         const uint32_t fx = mab[x];
-        for (int w = 0; w < W; w++) {
-          const int y = 32 * w + lane;
-          const bool c = y < x && conflict(nb, mab[y], fx);
-          const uint32_t word = __ballot_sync(kFull, c);
-          if (lane == 0) bits[x * W + w] = word;
+        for (int w0 = 0; w0 < W; w0 += 4) {
+          uint32_t word[4] = {0u, 0u, 0u, 0u};
+          if (32 * w0 < x) {  // words of members after x stay zero
+#pragma unroll
+            for (int d = 0; d < 4; d++) {
+              const int y = 32 * (w0 + d) + lane;  // mab is read for y < x < na only
+              word[d] = __ballot_sync(kFull, y < x && conflict(nb, mab[y], fx));
+            }
+          }
+          if (lane == 0) {
+#pragma unroll
+            for (int d = 0; d < 4; d++)
+              if (w0 + d < W) bits[x * W + w0 + d] = word[d];
+          }
         }
       }
       for (int w = tid; w < W; w += nt) {
@@ -386,38 +469,39 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       __syncthreads();
     }
     // ---- 4. filter the rest, compacting in place ----
-    K nmin = kmax_value<K>(), nmax = 0;
+    // Each step u of a warp stores its survivors contiguously (ballot
+    // ranks) after the warp's offset (one scan over the warps' totals).
     int base = 0;
-    constexpr int U = 4;
     for (int x0 = 0; x0 < m; x0 += U * nt) {
       K kv[U];
-      bool keep[U];
+      unsigned bal[U];
       int cnt = 0;
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const int x = x0 + u * nt + tid;
-        keep[u] = false;
-        if (x < m) {
-          kv[u] = list[x];
-          keep[u] = kv[u] > T && !killed(nb, footprint_of(nb, (uint32_t)kv[u]), cov, pw);
-        }
-        cnt += keep[u];
+        kv[u] = x < m ? list[x] : kmax_value<K>();
       }
-      int tot;
-      int o = base + block_scan_int(cnt, s_scan, tot);  // all loads of the chunk precede its stores
 #pragma unroll
       for (int u = 0; u < U; u++) {
-        if (!keep[u]) continue;
-        list[o++] = kv[u];
-        nmin = kv[u] < nmin ? kv[u] : nmin;
-        nmax = kv[u] > nmax ? kv[u] : nmax;
+        const int x = x0 + u * nt + tid;
+        const bool keep = x < m && kv[u] > T && !killed(nb, footprint_of(nb, (uint32_t)kv[u]), cov, pw);
+        bal[u] = __ballot_sync(kFull, keep);
+        cnt += __popc(bal[u]);
+      }
+      int tot;
+      int o = base + block_scan_warps(cnt, s_scan, tot);  // all loads of the chunk precede its stores
+      const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if ((bal[u] >> lane) & 1u) list[o + __popc(bal[u] & below)] = kv[u];
+        o += __popc(bal[u]);
       }
       base += tot;
     }
     m = base;
-    kmin = nmin;
-    kmax = nmax;
-    block_minmax(kmin, kmax, s_red);
+    lo = T + 1;
+    range = hi - lo;
+    sft = bin_shift(bitlen(range));
   }
   if (tid == 0) {
     J->tkcount[nb] = nk < kcap ? nk : kcap;

@@ -24,6 +24,8 @@ Beside the headline, in the same line:
   total      TOTAL multi-improvement at n = 1000 (every evaluated move a merge
              candidate): one pass per neighbourhood and a whole DVND, beside
              the oracle's CPU time for the same work
+  grasp      the multi-start constructor (MLSolution::random) on the device:
+             2048 starts at n = 1000, beside the oracle's CPU time per start
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -617,6 +619,42 @@ def bench_total(args, mlpgpu, workloads, stream, flush):
                                     "swap_cpu_graph_merge_ms": 17838.6}}
 
 
+def bench_grasp(args, mlpgpu, workloads):
+    """Multi-start constructor (MLSolution::random, alpha = 0.5) on the device:
+    2048 starts of the n = 1000 instance in one call (host seeds in, host tours
+    out), against the oracle's CPU restatements of the same constructor."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU-baseline leg of this workload, and its checker
+
+    n, count = N_NODES, args.grasp_starts
+    x, y = workloads.uniform_instance(n, INSTANCE_SEED)
+    p = mlpgpu.Problem.from_coords(x, y, dist_round=True)
+    seeds = np.arange(count, dtype=np.uint32)
+    p.random_tours(seeds[:8], 0.5)  # warm-up
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        tours = p.random_tours(seeds, 0.5)
+        times.append(time.perf_counter() - t0)
+    D = oracle.dist(x, y, True)
+    for q in range(4):
+        assert np.array_equal(tours[q], oracle.random_tour_canonical(D, int(seeds[q]), 0.5)), "constructor mismatch"
+    k = 8
+    c0 = time.perf_counter()
+    for q in range(k):
+        oracle.random_tour_canonical(D, q, 0.5)
+    c1 = time.perf_counter()
+    for q in range(k):
+        oracle.random_tour(D, q, 0.5)
+    c2 = time.perf_counter()
+    t = statistics.median(times)
+    return {"workload": f"{count} starts of MLSolution::random(alpha=0.5) for the n={n} instance, one call "
+                        "(seeds from the host, tours copied back)",
+            "seconds": t, "starts_per_s": count / t,
+            "cpu_oracle_ms_per_start": {"canonical_ties": (c1 - c0) / k * 1e3, "std_sort_ties": (c2 - c1) / k * 1e3,
+                                        "sample": f"{k} starts each, 1 thread"}}
+
+
 def run_ours(args, world, rank, local) -> None:
     import torch
 
@@ -637,7 +675,8 @@ def run_ours(args, world, rank, local) -> None:
         fn = {"batched": lambda: bench_batched(args, mlpgpu, workloads, stream),
               "serving": lambda: bench_serving(args, mlpgpu, workloads),
               "large": lambda: bench_large(args, mlpgpu, workloads, stream, flush),
-              "total": lambda: bench_total(args, mlpgpu, workloads, stream, flush)}[args.only]
+              "total": lambda: bench_total(args, mlpgpu, workloads, stream, flush),
+              "grasp": lambda: bench_grasp(args, mlpgpu, workloads)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}))
         return
@@ -660,6 +699,8 @@ def run_ours(args, world, rank, local) -> None:
             extra["large"] = bench_large(args, mlpgpu, workloads, stream, flush)
         if "total" in wl:
             extra["total"] = bench_total(args, mlpgpu, workloads, stream, flush)
+        if "grasp" in wl:
+            extra["grasp"] = bench_grasp(args, mlpgpu, workloads)
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -715,7 +756,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-iters", type=int, default=1 << 20)
-    ap.add_argument("--workloads", default="batched,serving,large,total",
+    ap.add_argument("--workloads", default="batched,serving,large,total,grasp",
                     help="extra workloads reported beside the plain n=1000 headline")
     ap.add_argument("--batch-instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=128)
@@ -726,8 +767,9 @@ def main() -> None:
     ap.add_argument("--large-n", type=int, default=10000)
     ap.add_argument("--large-iters", type=int, default=300)
     ap.add_argument("--total-reps", type=int, default=5)
+    ap.add_argument("--grasp-starts", type=int, default=2048)
     ap.add_argument("--total-cpu-iters", type=int, default=8)
-    ap.add_argument("--only", choices=["batched", "serving", "large", "total"], default=None,
+    ap.add_argument("--only", choices=["batched", "serving", "large", "total", "grasp"], default=None,
                     help="run one extra workload alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

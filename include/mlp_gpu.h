@@ -99,6 +99,11 @@ MLP_API int mlp_problem_create_matrix(int32_t n, const int32_t* dist, int32_t co
 MLP_API int mlp_problem_load_tsplib(const char* path, int32_t cost_tour, int32_t dist_round,
                                     mlp_problem_t* out);
 MLP_API int mlp_problem_info(mlp_problem_t p, int32_t* n, int32_t* size, int32_t* max_dist);
+/* `count` starts of MLSolution::random (as mlp_solver_random_tour), start q
+ * from seeds[q], built on the device in parallel (one warp each) and copied to
+ * `tours` (count x size entries, host memory). */
+MLP_API int mlp_problem_random_tours(mlp_problem_t p, int32_t count, const uint32_t* seeds, float alpha,
+                                     int32_t* tours);
 /* Copies the n x n distance matrix to host memory. */
 MLP_API int mlp_problem_get_dist(mlp_problem_t p, int32_t* dist);
 MLP_API void mlp_problem_destroy(mlp_problem_t p);
@@ -132,6 +137,13 @@ MLP_API int mlp_solver_set_total(mlp_solver_t s, int32_t on);
 MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len);
 /* Same with the tour already in device memory (enqueued, no host sync). */
 MLP_API int mlp_solver_set_tour_device(mlp_solver_t s, const int32_t* tour_dev, int32_t len);
+/* The tour becomes a start of MLSolution::random(rng, alpha) (source/mlsolution.cpp:754-874)
+ * built on the device: MTRandom seeded with `seed`; each step appends the
+ * candidate of rank rng.rand(ceil(alpha * count) - 1) in ascending distance to
+ * the client added last.  Equal distances are taken in client-id order (the
+ * reference's std::sort leaves their order to the library).  alpha in [0, 1].
+ * Rebuilds the ADS. */
+MLP_API int mlp_solver_random_tour(mlp_solver_t s, uint32_t seed, float alpha);
 MLP_API int mlp_solver_get_tour(mlp_solver_t s, int32_t* tour, int32_t len);
 /* Checkpoint / resume in the text format of MLSolution::save / load
  * (source/mlsolution.cpp:685-751): tour length, cost, the tour.  Loading
@@ -232,6 +244,9 @@ MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape);
  * 16 jobs or more, otherwise a six-CTA cluster per job), 1 = cluster, 2 = one
  * CTA per job.  Every mode gives the same results. */
 MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode);
+/* Adds a search whose start is MLSolution::random(seed, alpha), built on the
+ * device when the batch is (re)started (as mlp_solver_random_tour). */
+MLP_API int mlp_batch_add_random(mlp_batch_t b, mlp_problem_t p, uint32_t seed, float alpha, int32_t* job);
 /* Candidate mode of the batch's searches (as mlp_solver_set_total). */
 MLP_API int mlp_batch_set_total(mlp_batch_t b, int32_t on);
 /* Iterations between the host's convergence checks (default 16); after each

@@ -538,6 +538,38 @@ void orc_random_tour(int n, const int32_t* D, int costTour, uint32_t seed, float
   if (costTour) tour[len++] = 0;
 }
 
+// MLSolution::random (mlsolution.cpp:754-874) with a canonical order of
+// equal distances.  Both of the reference's branches pick the candidate of
+// ascending rank r = rng.rand(ceil(alpha * count) - 1) by distance to the
+// last client added (alpha < 0.5 sorts descending and takes position
+// count - r - 1); std::sort leaves the order of equal distances to the
+// library, so here the rank is taken in (distance, client id) order.
+void orc_random_tour_canonical(int n, const int32_t* D, uint32_t seed, float alpha, int32_t* tour) {
+  MT rng;
+  rng.seed(seed);
+  std::vector<int32_t> cands;
+  for (int c = 1; c < n; c++) cands.push_back(c);
+  int len = 0, last = 0;
+  tour[len++] = 0;
+  while (!cands.empty()) {
+    const uint32_t count = (uint32_t)cands.size();
+    uint32_t r = 0;
+    if (count > 1) {
+      const uint32_t rcl = (uint32_t)std::ceil(alpha * (float)count);
+      r = rcl > 0 ? rng.rand_max(rcl - 1) : 0;
+    }
+    const int32_t* row = D + (size_t)last * n;
+    std::nth_element(cands.begin(), cands.begin() + r, cands.end(), [row](int32_t a, int32_t b) {
+      return row[a] != row[b] ? row[a] < row[b] : a < b;
+    });
+    const int32_t cur = cands[r];
+    cands.erase(cands.begin() + r);
+    tour[len++] = cur;
+    last = cur;
+  }
+  tour[len++] = 0;
+}
+
 int64_t orc_cost(int size, const int32_t* tour, int n, const int32_t* D, int wide,
                  int32_t* w_out) {
   return cost_of(size, tour, n, D, wide, w_out);

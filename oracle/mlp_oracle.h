@@ -43,6 +43,9 @@ void orc_dist_from_coords(int n, const int32_t* x, const int32_t* y, int distRou
 /* ---- solution (source/mlsolution.cpp) ---- */
 /* MLSolution::random(rng(seed), alpha); writes `size` = n + costTour entries. */
 void orc_random_tour(int n, const int32_t* D, int costTour, uint32_t seed, float alpha, int32_t* tour);
+/* The same constructor with equal distances ordered by client id (the
+ * reference's std::sort leaves their order to the library); costTour = 1. */
+void orc_random_tour_canonical(int n, const int32_t* D, uint32_t seed, float alpha, int32_t* tour);
 /* update() + costCalc(): weights w[p] = D[t[p-1]][t[p]], cost = sum (size-p) w[p].
  * wide=0 returns the uint32 cost zero-extended. `w_out` may be NULL. */
 int64_t orc_cost(int size, const int32_t* tour, int n, const int32_t* D, int wide, int32_t* w_out);

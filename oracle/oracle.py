@@ -50,6 +50,7 @@ def lib() -> C.CDLL:
             "orc_tsplib_read": (i32, [C.c_char_p, i32, vp, vp]),
             "orc_dist_from_coords": (None, [i32, vp, vp, i32, vp]),
             "orc_random_tour": (None, [i32, vp, i32, C.c_uint32, C.c_float, vp]),
+            "orc_random_tour_canonical": (None, [i32, vp, C.c_uint32, C.c_float, vp]),
             "orc_cost": (i64, [i32, vp, i32, vp, i32, vp]),
             "orc_ads_build": (None, [i32, vp, i32, vp, vp, vp, i32, i32, vp]),
             "orc_num_blocks": (i32, [i32, i32]),
@@ -122,6 +123,15 @@ def random_tour(D: np.ndarray, seed: int, alpha: float = 0.5) -> np.ndarray:
     n = D.shape[0]
     t = np.zeros(n + 1, np.int32)
     lib().orc_random_tour(n, _p(D), 1, seed, C.c_float(alpha), _p(t))
+    return t
+
+
+def random_tour_canonical(D: np.ndarray, seed: int, alpha: float = 0.5) -> np.ndarray:
+    """MLSolution::random with equal distances ordered by client id."""
+    D = _i32(D)
+    n = D.shape[0]
+    t = np.zeros(n + 1, np.int32)
+    lib().orc_random_tour_canonical(n, _p(D), seed, C.c_float(alpha), _p(t))
     return t
 
 

@@ -29,7 +29,8 @@ struct mlp_batch {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<mlp::Job>> jobs;
-  std::vector<std::vector<int32_t>> tours;
+  std::vector<std::vector<int32_t>> tours;  // empty: the start is built on the device
+  std::vector<std::pair<uint32_t, float>> random_start;  // (seed, alpha) of those
   std::unique_ptr<mlp::JobSet> set;
   ~mlp_batch();
 };

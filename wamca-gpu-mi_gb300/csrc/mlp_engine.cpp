@@ -465,6 +465,47 @@ int default_shape(int size, int njobs) {
   return 3;                           // 64 x 4
 }
 
+// ---------------------------------------------------------------- constructor
+int check_alpha(float alpha) {
+  if (!(alpha >= 0.0f && alpha <= 1.0f)) {
+    set_error("alpha must lie in [0, 1]");
+    return kErrArg;
+  }
+  return kOk;
+}
+
+int build_random_tours(const std::vector<GraspTask>& tasks, cudaStream_t stream) {
+  if (tasks.empty()) return kOk;
+  struct Buffers {
+    GraspTask* tasks = nullptr;
+    int* err = nullptr;
+    ~Buffers() {
+      if (tasks) cudaFree(tasks);
+      if (err) cudaFree(err);
+    }
+  } b;
+  for (const GraspTask& t : tasks)
+    if (t.n < 1 || t.n > kMaxSize - 1 || !t.D || !t.tour) {
+      set_error("constructor task out of range");
+      return kErrArg;
+    }
+  MLP_CUDA(cudaMalloc(&b.tasks, sizeof(GraspTask) * tasks.size()), "cudaMalloc(constructor tasks)");
+  MLP_CUDA(cudaMalloc(&b.err, sizeof(int)), "cudaMalloc(constructor flag)");
+  MLP_CUDA(cudaMemcpyAsync(b.tasks, tasks.data(), sizeof(GraspTask) * tasks.size(), cudaMemcpyHostToDevice,
+                           stream),
+           "copy constructor tasks");
+  MLP_CUDA(cudaMemsetAsync(b.err, 0, sizeof(int), stream), "memset(constructor flag)");
+  MLP_CUDA(launch_grasp(b.tasks, (int)tasks.size(), b.err, stream), "constructor kernel");
+  int herr = 0;
+  MLP_CUDA(cudaMemcpyAsync(&herr, b.err, sizeof(int), cudaMemcpyDeviceToHost, stream), "read constructor flag");
+  MLP_CUDA(cudaStreamSynchronize(stream), "constructor");
+  if (herr) {
+    set_error("device constructor failed an internal check");
+    return kErrState;
+  }
+  return kOk;
+}
+
 // ---------------------------------------------------------------- JobSet
 JobSet::JobSet(std::vector<Job*> jobs, bool wide, cudaStream_t stream)
     : all_jobs_(jobs), jobs_(std::move(jobs)), wide_(wide), stream_(stream) {}

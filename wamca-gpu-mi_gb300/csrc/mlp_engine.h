@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "mlp_common.cuh"
+#include "mlp_kernels.cuh"
 
 namespace mlp {
 
@@ -189,6 +190,13 @@ class JobSet {
   cudaGraphExec_t loop_graph_ = nullptr;
   int loop_unroll_ = 0;
 };
+
+// Start tours of MLSolution::random built on the device (mlp_grasp.cu), one
+// per task, written to the tasks' device tours; waits for the stream and
+// reports a failed internal check.
+int build_random_tours(const std::vector<GraspTask>& tasks, cudaStream_t stream);
+// alpha of the constructor must lie in [0, 1].
+int check_alpha(float alpha);
 
 // Sweep tile shape for a job set whose largest tour has `size` positions:
 // the autotuner's table when one is set, else a built-in rule.

@@ -1,0 +1,198 @@
+// mlp_grasp.cu -- multi-start constructor on the device (sm_103a).
+//
+// MLSolution::random (source/mlsolution.cpp:754-874): a GRASP-style greedy
+// randomized construction.  From depot 0, each step draws
+//   r = rng.rand(ceil(alpha * count) - 1)          (MTRandom, source/mtrand.h:193-195)
+// and appends the candidate of ascending rank r by distance to the client
+// added last (both of the reference's branches select that rank: alpha < 0.5
+// sorts descending and takes position count - r - 1).  The reference's
+// std::sort leaves the order of equal distances to the library; here the
+// rank is taken in (distance, client id) order.  costTour: depot 0 closes the
+// tour.
+//
+// One warp builds one start.  MT19937 (source/mtrand.cpp:52-124) runs on
+// lane 0 with its state in shared memory; the remaining candidates live in
+// the tail of the tour being built, tour[len..n), and each step selects rank
+// r among them with a three-level radix select (10-bit digits of the 30-bit
+// key distance << 14 | id) over a per-warp 1024-bin histogram, then swaps the
+// selected candidate to tour[len].
+#include <cmath>
+#include <cstdint>
+
+#include "mlp_common.cuh"
+#include "mlp_kernels.cuh"
+
+namespace mlp {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kGraspWarps = 8;  // starts per CTA
+constexpr int kMtN = 624, kMtM = 397;
+
+struct GraspSmem {
+  static constexpr size_t mt = 0;                              // uint32[kMtN] per warp
+  static constexpr size_t hist = (size_t)kMtN * 4;             // uint32[1024] per warp
+  static constexpr size_t per_warp = hist + 1024 * 4;
+  static constexpr size_t total = per_warp * kGraspWarps;
+};
+
+// MTRandom::seed (mtrand.cpp:52-61)
+__device__ void mt_seed(uint32_t* st, uint32_t s) {
+  st[0] = s;
+  for (int p = 1; p < kMtN; p++) st[p] = 1812433253u * (st[p - 1] ^ (st[p - 1] >> 30)) + (uint32_t)p;
+}
+
+// MTRandom::gen (mtrand.cpp:99-124)
+__device__ void mt_gen(uint32_t* st) {
+  int i = 0;
+  uint32_t y;
+  for (; i < kMtN - kMtM; i++) {
+    y = (st[i] & 0x80000000u) | (st[i + 1] & 0x7fffffffu);
+    st[i] = st[i + kMtM] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+  }
+  for (; i < kMtN - 1; i++) {
+    y = (st[i] & 0x80000000u) | (st[i + 1] & 0x7fffffffu);
+    st[i] = st[i + (kMtM - kMtN)] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+  }
+  y = (st[kMtN - 1] & 0x80000000u) | (st[0] & 0x7fffffffu);
+  st[kMtN - 1] = st[kMtM - 1] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+}
+
+// MTRandom::rand() with tempering (mtrand.h:167-179); *pos is the state index.
+__device__ uint32_t mt_rand(uint32_t* st, int* pos) {
+  if (*pos >= kMtN) {
+    mt_gen(st);
+    *pos = 0;
+  }
+  uint32_t x = st[(*pos)++];
+  x ^= (x >> 11);
+  x ^= (x << 7) & 0x9d2c5680u;
+  x ^= (x << 15) & 0xefc60000u;
+  return x ^ (x >> 18);
+}
+
+// MTRandom::rand(max) (mtrand.h:193-195): IEEE double multiply and divide,
+// as on the host.
+__device__ uint32_t mt_rand_max(uint32_t* st, int* pos, uint32_t mx) {
+  const double v = __dmul_rn((double)mx + 1.0, (double)mt_rand(st, pos));
+  return (uint32_t)__ddiv_rn(v, 4294967296.0);
+}
+
+__device__ __forceinline__ uint32_t grasp_key(const int32_t* __restrict__ row, int32_t c) {
+  return ((uint32_t)row[c] << 14) | (uint32_t)c;
+}
+
+__global__ void __launch_bounds__(32 * kGraspWarps)
+    k_grasp(const GraspTask* __restrict__ tasks, int count, int* __restrict__ err) {
+  extern __shared__ __align__(16) uint8_t gsm[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int start = blockIdx.x * kGraspWarps + wid;
+  if (start >= count) return;  // whole warps only
+  const GraspTask task = tasks[start];
+  const int32_t* __restrict__ D = task.D;
+  const int n = task.n;
+  const float alpha = task.alpha;
+  uint32_t* st = (uint32_t*)(gsm + wid * GraspSmem::per_warp + GraspSmem::mt);
+  uint32_t* hist = (uint32_t*)(gsm + wid * GraspSmem::per_warp + GraspSmem::hist);
+  int32_t* t = task.tour;
+  int pos = kMtN;
+  if (lane == 0) mt_seed(st, task.seed);
+  for (int p = lane; p < n; p += 32) t[p] = p;  // t[0] = depot, candidates 1..n-1 after it
+  if (lane == 0) t[n] = 0;
+  __syncwarp();
+  int last = 0;
+  for (int len = 1; len < n; len++) {
+    const int cnt = n - len;
+    uint32_t r = 0;
+    if (lane == 0 && cnt > 1) {
+      const uint32_t rcl = (uint32_t)ceilf(__fmul_rn(alpha, (float)cnt));
+      r = rcl > 0 ? mt_rand_max(st, &pos, rcl - 1) : 0u;
+    }
+    r = __shfl_sync(kFull, r, 0);
+    if (r >= (uint32_t)cnt) r = cnt - 1;  // alpha <= 1 (checked by the host) keeps r < cnt
+    const int32_t* __restrict__ row = D + (size_t)last * n;
+    // rank r among the keys of t[len..n): three 10-bit digits, high first
+    uint32_t prefix = 0;
+#pragma unroll 1
+    for (int lvl = 0; lvl < 3; lvl++) {
+      const int sft = 20 - 10 * lvl;
+      for (int q = lane; q < 1024; q += 32) hist[q] = 0;
+      __syncwarp();
+      for (int p = len + lane; p < n; p += 32) {
+        const uint32_t k = grasp_key(row, t[p]);
+        if (lvl == 0 || (k >> (sft + 10)) == prefix) atomicAdd(&hist[(k >> sft) & 1023u], 1u);
+      }
+      __syncwarp();
+      // lane l owns bins 32l .. 32l+31
+      uint32_t own = 0;
+      for (int q = 0; q < 32; q++) own += hist[32 * lane + q];
+      uint32_t inc = own;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += y;
+      }
+      const uint32_t exc = inc - own;
+      const unsigned hit = __ballot_sync(kFull, r >= exc && r < inc);
+      const int src = __ffs(hit) - 1;  // the lane whose bins hold rank r
+      uint32_t digit = 0, below = 0;
+      if (lane == src) {
+        uint32_t acc = exc;
+        for (int q = 0; q < 32; q++) {
+          const uint32_t h = hist[32 * lane + q];
+          if (r < acc + h) {
+            digit = 32u * lane + q;
+            below = acc;
+            break;
+          }
+          acc += h;
+        }
+      }
+      digit = __shfl_sync(kFull, digit, src);
+      below = __shfl_sync(kFull, below, src);
+      r -= below;
+      prefix = (prefix << 10) | digit;
+      __syncwarp();  // hist is cleared by the next level
+    }
+    // The selected candidate (keys are distinct: ids are) moves to t[len].
+    int found = -1;
+    for (int p0 = len; p0 < n; p0 += 32) {
+      const int p = p0 + lane;
+      const bool m = p < n && grasp_key(row, t[p]) == prefix;
+      const unsigned b = __ballot_sync(kFull, m);
+      if (b) {
+        found = p0 + __ffs(b) - 1;
+        break;
+      }
+    }
+    const int32_t cur = (int32_t)(prefix & 0x3fffu);
+    if (found < 0) {  // unreachable (the rank-r key exists); t stays a permutation
+      if (lane == 0) atomicAdd(err, 1);
+      return;
+    }
+    if (lane == 0) {
+      t[found] = t[len];
+      t[len] = cur;
+    }
+    __syncwarp();
+    last = cur;
+  }
+}
+
+}  // namespace
+
+cudaError_t configure_grasp() {
+  return cudaFuncSetAttribute(k_grasp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GraspSmem::total);
+}
+
+cudaError_t launch_grasp(const GraspTask* tasks, int count, int* err, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  const cudaError_t e = configure_grasp();
+  if (e != cudaSuccess) return e;
+  const int grid = (count + kGraspWarps - 1) / kGraspWarps;
+  k_grasp<<<grid, 32 * kGraspWarps, GraspSmem::total, s>>>(tasks, count, err);
+  return cudaGetLastError();
+}
+
+}  // namespace mlp

@@ -69,6 +69,20 @@ cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool u
                                 cudaStream_t s);
 // Opt the TOTAL greedy into its dynamic shared memory (configure_merge calls it).
 cudaError_t configure_total();
+// MLSolution::random on the device (mlp_grasp.cu): one start per task, its
+// n + 1 entries written to `tour` (device), MTRandom seeded with `seed`,
+// equal distances ordered by client id; alpha in [0, 1].  *err (device)
+// counts starts that failed an internal check (none expected).
+struct GraspTask {
+  const int32_t* D;  // n x n distances
+  int32_t* tour;     // n + 1 entries
+  int32_t n;
+  uint32_t seed;
+  float alpha;
+  int32_t pad;
+};
+cudaError_t configure_grasp();
+cudaError_t launch_grasp(const GraspTask* tasks, int count, int* err, cudaStream_t s);
 // Reference ADS buffer (source/mlads.h:38-74) of each job's current tour.
 cudaError_t launch_ads(const JobDev* job, const int32_t* cx, const int32_t* cy, uint32_t* ads,
                        int cost_tour, int dist_round, cudaStream_t s, uint32_t* Pbuf, int size);

@@ -26,6 +26,7 @@ Beside the headline, in the same line:
              the oracle's CPU time for the same work
   grasp      the multi-start constructor (MLSolution::random) on the device:
              2048 starts at n = 1000, beside the oracle's CPU time per start
+  oropt_k    Or-opt-k for k = 4, 8, 16, 28 at n = 1000: candidates and a pass
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -655,6 +656,40 @@ def bench_grasp(args, mlpgpu, workloads):
                                         "sample": f"{k} starts each, 1 thread"}}
 
 
+def bench_oropt_k(args, mlpgpu, workloads, stream):
+    """Or-opt-k beyond the DVND's k = 1, 2, 3 (MLKernelOrOpt(problem, k)): the
+    per-block candidates of one neighbourhood (device time of the evaluation
+    call: ADS refresh, one CTA per reference block, key reset) on the n = 1000
+    instance, and one pass of it."""
+    import torch
+
+    n = N_NODES
+    x, y = workloads.uniform_instance(n, INSTANCE_SEED)
+    s = mlpgpu.Solver(mlpgpu.Problem.from_coords(x, y, dist_round=True))
+    s.set_stream(stream.cuda_stream)
+    t0 = workloads.random_perm_tour(n, 7)
+    out = {}
+    for k in (4, 8, 16, 28):
+        s.set_tour(t0)
+        for _ in range(3):
+            s.eval_oropt(k)
+        times = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            c0 = time.perf_counter()
+            s.eval_oropt(k)
+            times.append(time.perf_counter() - c0)
+        m = n + 1 - k - 2
+        t = statistics.median(times)
+        c1 = time.perf_counter()
+        _, moves = s.pass_oropt(k)
+        tp = time.perf_counter() - c1
+        out[f"k{k}"] = {"evals": m * m, "eval_call_ms": t * 1e3, "evals_per_s": m * m / t, "pass_call_ms": tp * 1e3,
+                        "moves_applied": len(moves)}
+    return {"workload": f"n={n} uniform, seeded random start; host-timed calls (including the candidate copy)",
+            **out}
+
+
 def run_ours(args, world, rank, local) -> None:
     import torch
 
@@ -676,7 +711,8 @@ def run_ours(args, world, rank, local) -> None:
               "serving": lambda: bench_serving(args, mlpgpu, workloads),
               "large": lambda: bench_large(args, mlpgpu, workloads, stream, flush),
               "total": lambda: bench_total(args, mlpgpu, workloads, stream, flush),
-              "grasp": lambda: bench_grasp(args, mlpgpu, workloads)}[args.only]
+              "grasp": lambda: bench_grasp(args, mlpgpu, workloads),
+              "oropt_k": lambda: bench_oropt_k(args, mlpgpu, workloads, stream)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}))
         return
@@ -701,6 +737,8 @@ def run_ours(args, world, rank, local) -> None:
             extra["total"] = bench_total(args, mlpgpu, workloads, stream, flush)
         if "grasp" in wl:
             extra["grasp"] = bench_grasp(args, mlpgpu, workloads)
+        if "oropt_k" in wl:
+            extra["oropt_k"] = bench_oropt_k(args, mlpgpu, workloads, stream)
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -756,7 +794,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-iters", type=int, default=1 << 20)
-    ap.add_argument("--workloads", default="batched,serving,large,total,grasp",
+    ap.add_argument("--workloads", default="batched,serving,large,total,grasp,oropt_k",
                     help="extra workloads reported beside the plain n=1000 headline")
     ap.add_argument("--batch-instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=128)
@@ -769,7 +807,7 @@ def main() -> None:
     ap.add_argument("--total-reps", type=int, default=5)
     ap.add_argument("--grasp-starts", type=int, default=2048)
     ap.add_argument("--total-cpu-iters", type=int, default=8)
-    ap.add_argument("--only", choices=["batched", "serving", "large", "total", "grasp"], default=None,
+    ap.add_argument("--only", choices=["batched", "serving", "large", "total", "grasp", "oropt_k"], default=None,
                     help="run one extra workload alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

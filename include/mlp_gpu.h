@@ -172,6 +172,16 @@ MLP_API int mlp_solver_eval(mlp_solver_t s, int32_t nb, int64_t* cost, int32_t* 
 MLP_API int mlp_solver_pass(mlp_solver_t s, int32_t nb, int32_t max_moves, int32_t* ids,
                             int32_t* is, int32_t* js, int64_t* costs, int32_t* count,
                             int64_t* new_cost);
+/* Or-opt-k for any k in [1, 28] (MLKernelOrOpt(problem, k): the ODC
+ * kernelOrOpt with tag = k, source/mlkoropt.cu:620-794, move id k + 1).
+ * eval: the per-block candidates, size - k - 2 entries (as mlp_solver_eval).
+ * pass: evaluate, merge the improving candidates greedily in (delta, block)
+ * order with f_canOrOptMerge, apply them and rebuild the ADS (as
+ * mlp_solver_pass); moves are written in application order, their id is
+ * k + 1.  The DVND's three Or-opt neighbourhoods are k = 1, 2, 3. */
+MLP_API int mlp_solver_eval_oropt(mlp_solver_t s, int32_t k, int64_t* cost, int32_t* i, int32_t* j);
+MLP_API int mlp_solver_pass_oropt(mlp_solver_t s, int32_t k, int32_t max_moves, int32_t* is, int32_t* js,
+                                  int64_t* costs, int32_t* count, int64_t* new_cost);
 /* Multi-improvement DVND to a local optimum over the neighbourhoods of nb_mask
  * (at most max_iters sweeps).  Synchronous. */
 MLP_API int mlp_solver_dvnd(mlp_solver_t s, int32_t nb_mask, int32_t max_iters,

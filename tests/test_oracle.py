@@ -180,3 +180,18 @@ def test_solution_checkpoint_text_format(tmp_path, berlin):
     (tmp_path / "bad.txt").write_text("53\n1\n0 1 2\n")
     with pytest.raises(ValueError):
         mlpgpu.load_solution(str(tmp_path / "bad.txt"))
+
+
+@pytest.mark.parametrize("k", [1, 4, 9, 15, 28])
+def test_oropt_k_deltas_any_k(k):
+    # Or-opt-k of any k in [1, 28] (MLKernelOrOpt(problem, k), move id k + 1):
+    # the oracle's per-block candidates match brute force (apply + costCalc).
+    n = 70
+    x, y = oracle.uniform_instance(n, 30 + k)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, 30 + k)
+    nb = k + 1
+    c, i, j, _ = oracle.eval_nb(nb, t, D)
+    assert len(c) == n + 1 - k - 2
+    for b in range(len(c)):
+        assert c[b] == oracle.move_delta(nb, int(i[b]), int(j[b]), t, D, brute=True)

@@ -437,6 +437,91 @@ MLP_API int mlp_solver_eval(mlp_solver_t s, int32_t nb, int64_t* cost, int32_t* 
   return kOk;
 }
 
+static int oropt_k_check(mlp_solver_t s, int32_t k) {
+  if (!s) return arg_error("null solver");
+  if (k < 1 || k > kMaxOroptK) return arg_error("Or-opt k must lie in [1, 28]");
+  if (oropt_blocks(k, s->prob->size) < 1) return arg_error("Or-opt k too large for this instance");
+  return kOk;
+}
+
+// Per-block candidates of Or-opt-k into the job's key array (keys reset by
+// the caller's prepare afterwards).
+static int oropt_eval_keys(mlp_solver_t s, int32_t k) {
+  MLP_TRY(s->set->prepare(false));
+  MLP_CUDA(launch_oropt_eval(s->set->device_jobs(), k, s->prob->size, s->wide, s->job->dev.keys, s->set->stream()),
+           "Or-opt-k kernel");
+  return kOk;
+}
+
+MLP_API int mlp_solver_eval_oropt(mlp_solver_t s, int32_t k, int64_t* cost, int32_t* oi, int32_t* oj) {
+  MLP_TRY(oropt_k_check(s, k));
+  if (!cost || !oi || !oj) return arg_error("null argument");
+  const int sz = s->prob->size, m = oropt_blocks(k, sz);
+  MLP_TRY(oropt_eval_keys(s, k));
+  std::vector<uint64_t> keys(m);
+  MLP_CUDA(cudaMemcpyAsync(keys.data(), s->job->dev.keys, sizeof(uint64_t) * m, cudaMemcpyDeviceToHost,
+                           s->set->stream()),
+           "copy keys");
+  MLP_TRY(s->set->prepare(false));
+  MLP_CUDA(cudaStreamSynchronize(s->set->stream()), "sync");
+  const int64_t sentinel = s->wide ? INT64_MAX : (int64_t)kCostInfty32;
+  for (int b = 0; b < m; b++) {
+    if (keys[b] == kKeyNone) {
+      cost[b] = sentinel;
+      oi[b] = oj[b] = 0;
+      continue;
+    }
+    int i, j;
+    map_oropt(k, sz, b, (int)(keys[b] & ((1u << kCtxBits) - 1)), i, j);
+    cost[b] = key_cost(keys[b], kCtxBits);
+    oi[b] = i;
+    oj[b] = j;
+  }
+  return kOk;
+}
+
+MLP_API int mlp_solver_pass_oropt(mlp_solver_t s, int32_t k, int32_t max_moves, int32_t* is, int32_t* js,
+                                  int64_t* costs, int32_t* count, int64_t* new_cost) {
+  MLP_TRY(oropt_k_check(s, k));
+  if (max_moves > 0 && (!is || !js || !costs)) return arg_error("null move arrays");
+  const int sz = s->prob->size, m = oropt_blocks(k, sz);
+  struct Scratch {
+    uint8_t* p = nullptr;
+    ~Scratch() {
+      if (p) cudaFree(p);
+    }
+  } sc;
+  const size_t body = oropt_pass_scratch_bytes(sz, k);
+  const size_t o_ij = (body + 255) / 256 * 256, o_cost = o_ij + ((size_t)m * 4 + 255) / 256 * 256;
+  const size_t o_cnt = o_cost + (size_t)m * 8, bytes = o_cnt + 256;
+  MLP_CUDA(cudaMalloc(&sc.p, bytes), "cudaMalloc(Or-opt-k pass)");
+  MLP_TRY(oropt_eval_keys(s, k));
+  uint32_t* dij = (uint32_t*)(sc.p + o_ij);
+  int64_t* dcost = (int64_t*)(sc.p + o_cost);
+  int* dcnt = (int*)(sc.p + o_cnt);
+  MLP_CUDA(launch_oropt_pass(s->set->device_jobs(), k, s->wide, s->job->dev.keys, sc.p, dij, dcost, dcnt,
+                             s->set->stream()),
+           "Or-opt-k pass kernel");
+  MLP_TRY(s->set->prepare(false));  // w, prefix arrays and cost of the new tour; keys reset
+  int applied = 0;
+  MLP_CUDA(cudaMemcpyAsync(&applied, dcnt, sizeof(int), cudaMemcpyDeviceToHost, s->set->stream()), "copy count");
+  MLP_CUDA(cudaStreamSynchronize(s->set->stream()), "sync");
+  const int take = std::min(applied, std::max(0, (int)max_moves));
+  if (take > 0) {
+    std::vector<uint32_t> mv(take);
+    MLP_CUDA(cudaMemcpyAsync(mv.data(), dij, 4 * take, cudaMemcpyDeviceToHost, s->set->stream()), "copy moves");
+    MLP_CUDA(cudaMemcpyAsync(costs, dcost, 8 * take, cudaMemcpyDeviceToHost, s->set->stream()), "copy moves");
+    MLP_CUDA(cudaStreamSynchronize(s->set->stream()), "sync");
+    for (int q = 0; q < take; q++) {
+      is[q] = (int32_t)(mv[q] & 0x3fff);
+      js[q] = (int32_t)(mv[q] >> 14);
+    }
+  }
+  if (count) *count = applied;
+  if (new_cost) MLP_TRY(mlp_solver_cost(s, new_cost));
+  return kOk;
+}
+
 MLP_API int mlp_solver_pass(mlp_solver_t s, int32_t nb, int32_t max_moves, int32_t* ids, int32_t* is,
                             int32_t* js, int64_t* costs, int32_t* count, int64_t* new_cost) {
   if (!s) return arg_error("null solver");

@@ -75,6 +75,22 @@ MLP_HD void map_move(int nb, int size, int by, int ctx, int& i, int& j) {
   }
 }
 
+// Or-opt-k for any k in [1, kMaxOroptK] (MLKernelOrOpt(problem, k), the
+// kernel's tag = k; move id k + 1, source/mlads.h:26-27): reference blocks
+// (= candidates) and the ODC block mapping, costTour = 1
+// (source/mlkoropt.cu:699-722, :842).
+constexpr int kMaxOroptK = 28;  // launchKernel rejects k > MLP_MAX_NEIGHBOR - 2 (mlkoropt.cu:866-868)
+MLP_HD int oropt_blocks(int k, int size) { return size - k - 2; }
+MLP_HD void map_oropt(int k, int size, int by, int ctx, int& i, int& j) {
+  if (ctx >= by) {
+    i = ctx - by + 1;
+    j = ctx + 2;
+  } else {
+    i = size - ctx - k - 1;
+    j = by - ctx;
+  }
+}
+
 MLP_HD uint64_t make_key(int64_t delta, uint32_t low, int low_bits) {
   return ((uint64_t)(delta + (int64_t)kCostBias) << low_bits) | (uint64_t)low;
 }

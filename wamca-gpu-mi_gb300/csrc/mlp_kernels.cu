@@ -609,9 +609,8 @@ __device__ __forceinline__ int group_sync_or(int pred, int id, int nthreads) {
 //              are small: the first alive candidate is kept and its conflicts
 //              removed, repeatedly.
 // On return st[x] == kIn marks the kept candidates.
-__device__ void stage2_group(int nb, int sz, int gtid, int gnt, int bar, Rec* rec, uint64_t* tables,
+__device__ void stage2_group(int nb, int sz, int m, int gtid, int gnt, int bar, Rec* rec, uint64_t* tables,
                              uint64_t* gmin) {
-  const int m = nb_blocks(nb, sz);
   if (nb == 0) {
     uint64_t* minK = tables;
     uint64_t* minB = tables + (sz + 4);
@@ -952,7 +951,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
       stage2_records(J, nb, sz, rec, ij);
       if (tid == 0) s_cnt = 0;
       __syncthreads();
-      stage2_group(nb, sz, tid, nt, 1, rec, (uint64_t*)(ws + lay.o_tab), s_gmin);
+      stage2_group(nb, sz, m, tid, nt, 1, rec, (uint64_t*)(ws + lay.o_tab), s_gmin);
       __syncthreads();
       // Write the kept moves into this neighbourhood's region of the leader.
       int nmine = 0;
@@ -1117,7 +1116,7 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
     const int m = nb_blocks(nb, sz);
     stage2_records(J, nb, sz, rec, ij);
     __syncthreads();
-    stage2_group(nb, sz, tid, nt, 1, rec, (uint64_t*)(ws + lay.o_tab), s_gmin);
+    stage2_group(nb, sz, m, tid, nt, 1, rec, (uint64_t*)(ws + lay.o_tab), s_gmin);
     __syncthreads();
     int nmine = 0;
     for (int x = tid; x < m; x += nt) nmine += rec[x].st == kIn;
@@ -1146,6 +1145,135 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
   __syncthreads();
   merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
                      t_old, (int32_t*)(ws + lay.o_tnew));
+}
+
+// --------------------------------------------------------------------------
+// Or-opt-k for any k in [1, 28] (MLKernelOrOpt(problem, k)): the reference's
+// ODC kernelOrOpt with tag = k (source/mlkoropt.cu:620-794) and its runKernel
+// pass (GPU merge with f_canOrOptMerge, mlkernel.cu:61-71, 73-170; applyMove,
+// mlkoropt.cu:896-925).  The five-slot DVND keeps k = 1, 2, 3 in its fused
+// sweep; these kernels serve any single Or-opt-k neighbourhood.
+// --------------------------------------------------------------------------
+// Delta of Or-opt-k move (i, j) from the prefix sums (same formulas as the
+// sweep's, with the distances gathered from D; mlkoropt.cu:704-716, :724-736).
+template <bool WIDE>
+__device__ typename Arith<WIDE>::V oropt_delta(const JobDev* J, int k, int i, int j) {
+  using C = typename Arith<WIDE>::C;
+  const int32_t* __restrict__ t = J->tour;
+  const int32_t* __restrict__ D = J->D;
+  const int32_t* __restrict__ w = J->w;
+  const C* __restrict__ W = (const C*)J->W;
+  const int n = J->n;
+  auto d = [&](int a, int b) -> C { return (C)D[(size_t)t[a] * n + t[b]]; };
+  auto R = [&](int a, int b) -> C { return a > b ? C(0) : C(W[b] - W[a - 1]); };
+  const C sz = (C)J->size, kc = (C)k, ic = (C)i, jc = (C)j;
+  C c;
+  if (i < j)
+    c = (sz - ic) * (d(i - 1, i + k) - (C)w[i]) + (sz - jc - kc) * (d(i + k - 1, j + k) - (C)w[j + k]) +
+        (sz - jc) * d(j + k - 1, i) - (sz - ic - kc) * (C)w[i + k] + (ic - jc) * R(i + 1, i + k - 1) +
+        kc * R(i + k + 1, j + k - 1);
+  else
+    c = (sz - jc) * (d(j - 1, i) - (C)w[j]) + (sz - ic - kc) * (d(i - 1, i + k) - (C)w[i + k]) +
+        (sz - jc - kc) * d(i + k - 1, j) - (sz - ic) * (C)w[i] + (ic - jc) * R(i + 1, i + k - 1) -
+        kc * R(j + 1, i - 1);
+  return (typename Arith<WIDE>::V)c;
+}
+
+// One CTA per reference block: the block's best move as a (delta, ctx) key
+// (strict minimum, first ctx on ties; a delta equal to COST_INFTY never
+// wins, as in the reference's chunk loop).
+template <bool WIDE>
+__global__ void __launch_bounds__(256) k_oropt_eval(const JobDev* __restrict__ J, int k, uint64_t* __restrict__ keys) {
+  __shared__ uint64_t s_min[8];
+  const int by = blockIdx.x, sz = J->size, nthr = oropt_blocks(k, sz);
+  uint64_t best = kKeyNone;
+  for (int ctx = threadIdx.x; ctx < nthr; ctx += blockDim.x) {
+    int i, j;
+    map_oropt(k, sz, by, ctx, i, j);
+    const typename Arith<WIDE>::V d = oropt_delta<WIDE>(J, k, i, j);
+    if (d == Arith<WIDE>::kInf) continue;
+    const uint64_t key = make_key((int64_t)d, (uint32_t)ctx, kCtxBits);
+    best = key < best ? key : best;
+  }
+  best = warp_min_u64(best);
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) best = s_min[w] < best ? s_min[w] : best;
+    best = s_min[0] < best ? s_min[0] : best;
+    keys[by] = best;
+  }
+}
+
+// The pass: improving block candidates in (delta, block) order, greedily
+// independent under f_canOrOptMerge (closed intervals [min, max + k] must not
+// meet), applied together (disjoint footprints).  Writes the new tour and the
+// kept moves in order (ij: i | j << 14, cost) with their count; the caller
+// rebuilds the ADS arrays afterwards.  One CTA; scratch: m records, m ij
+// words, and size words each for the owner map and the old tour.
+template <bool WIDE>
+__global__ void __launch_bounds__(1024) k_oropt_pass(const JobDev* __restrict__ J, int k, const uint64_t* keys,
+                                                     uint8_t* scratch, uint32_t* out_ij, int64_t* out_cost,
+                                                     int* out_count) {
+  __shared__ uint64_t s_gmin[64];
+  __shared__ int s_cnt;
+  const int sz = J->size, m = oropt_blocks(k, sz), tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  const int id = k + 1;
+  Rec* rec = (Rec*)scratch;
+  uint32_t* ij = (uint32_t*)(scratch + align_up((size_t)m * sizeof(Rec), 16));
+  int32_t* owner = (int32_t*)((uint8_t*)ij + align_up((size_t)m * 4, 16));
+  int32_t* t_old = (int32_t*)((uint8_t*)owner + align_up((size_t)sz * 4, 16));
+  int32_t* tour = J->tour;
+  for (int b = tid; b < m; b += nt) {
+    Rec r;
+    r.key = kKeyNone;
+    r.ab = 0;
+    r.st = kNone;
+    const uint64_t key = keys[b];
+    if (key != kKeyNone) {
+      const int64_t cost = key_cost(key, kCtxBits);
+      if (cost < 0) {
+        int i, j;
+        map_oropt(k, sz, b, (int)(key & ((1u << kCtxBits) - 1)), i, j);
+        r.key = make_key(cost, (uint32_t)b, kCtxBits);
+        r.ab = (uint32_t)imin_(i, j) | ((uint32_t)(imax_(i, j) + k) << 16);
+        r.st = kUndec;
+        ij[b] = (uint32_t)i | ((uint32_t)j << 16);
+      }
+    }
+    rec[b] = r;
+  }
+  for (int p = tid; p < sz; p += nt) {
+    t_old[p] = tour[p];
+    owner[p] = -1;
+  }
+  if (tid == 0) s_cnt = 0;
+  __syncthreads();
+  stage2_group(2, sz, m, tid, nt, 1, rec, nullptr, s_gmin);  // the interval branch
+  __syncthreads();
+  for (int x = wid; x < m; x += nw) {
+    if (rec[x].st != kIn) continue;
+    const int i = (int)(ij[x] & 0xffff), j = (int)(ij[x] >> 16);
+    int f0, f1;
+    move_footprint(id, i, j, f0, f1);
+    for (int p = f0 + lane; p <= f1; p += 32) owner[p] = x;
+    if (lane == 0) atomicAdd(&s_cnt, 1);
+  }
+  __syncthreads();
+  for (int p = tid; p < sz; p += nt) {
+    const int o = owner[p];
+    if (o >= 0) tour[p] = t_old[move_source(id, (int)(ij[o] & 0xffff), (int)(ij[o] >> 16), p)];
+  }
+  for (int x = tid; x < m; x += nt) {
+    if (rec[x].st != kIn) continue;
+    int rank = 0;
+    for (int y = 0; y < m; y++)
+      if (rec[y].st == kIn && rec[y].key < rec[x].key) rank++;
+    out_ij[rank] = (ij[x] & 0xffff) | ((ij[x] >> 16) << 14);
+    out_cost[rank] = key_cost(rec[x].key, kCtxBits);
+  }
+  if (tid == 0) *out_count = s_cnt;
 }
 
 // --------------------------------------------------------------------------
@@ -1428,6 +1556,26 @@ cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool u
   const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
   if (wide) k_total_finish<true><<<njobs, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
   else k_total_finish<false><<<njobs, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  return cudaGetLastError();
+}
+
+size_t oropt_pass_scratch_bytes(int size, int k) {
+  const int m = oropt_blocks(k, size);
+  return align_up((size_t)m * sizeof(Rec), 16) + align_up((size_t)m * 4, 16) + 2 * align_up((size_t)size * 4, 16);
+}
+
+cudaError_t launch_oropt_eval(const JobDev* job, int k, int size, bool wide, uint64_t* keys, cudaStream_t s) {
+  const int m = oropt_blocks(k, size);
+  if (m <= 0) return cudaErrorInvalidValue;
+  if (wide) k_oropt_eval<true><<<m, 256, 0, s>>>(job, k, keys);
+  else k_oropt_eval<false><<<m, 256, 0, s>>>(job, k, keys);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_oropt_pass(const JobDev* job, int k, bool wide, const uint64_t* keys, uint8_t* scratch,
+                              uint32_t* out_ij, int64_t* out_cost, int* out_count, cudaStream_t s) {
+  if (wide) k_oropt_pass<true><<<1, 1024, 0, s>>>(job, k, keys, scratch, out_ij, out_cost, out_count);
+  else k_oropt_pass<false><<<1, 1024, 0, s>>>(job, k, keys, scratch, out_ij, out_cost, out_count);
   return cudaGetLastError();
 }
 

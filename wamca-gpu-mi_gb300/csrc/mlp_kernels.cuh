@@ -83,6 +83,13 @@ struct GraspTask {
 };
 cudaError_t configure_grasp();
 cudaError_t launch_grasp(const GraspTask* tasks, int count, int* err, cudaStream_t s);
+// Or-opt-k for any k in [1, kMaxOroptK] on one job: the per-block candidates
+// (oropt_blocks(k, size) keys, (delta, ctx) as the sweep's) and the pass over
+// them (greedy, apply; rebuild the ADS afterwards with launch_prepare).
+size_t oropt_pass_scratch_bytes(int size, int k);
+cudaError_t launch_oropt_eval(const JobDev* job, int k, int size, bool wide, uint64_t* keys, cudaStream_t s);
+cudaError_t launch_oropt_pass(const JobDev* job, int k, bool wide, const uint64_t* keys, uint8_t* scratch,
+                              uint32_t* out_ij, int64_t* out_cost, int* out_count, cudaStream_t s);
 // Reference ADS buffer (source/mlads.h:38-74) of each job's current tour.
 cudaError_t launch_ads(const JobDev* job, const int32_t* cx, const int32_t* cy, uint32_t* ads,
                        int cost_tour, int dist_round, cudaStream_t s, uint32_t* Pbuf, int size);

@@ -96,6 +96,8 @@ def lib() -> C.CDLL:
         "mlp_solver_set_tile_shape": (C.c_int, [vp, i32]),
         "mlp_solver_set_unroll": (C.c_int, [vp, i32]),
         "mlp_solver_set_total": (C.c_int, [vp, i32]),
+        "mlp_solver_eval_oropt": (C.c_int, [vp, i32, vp, vp, vp]),
+        "mlp_solver_pass_oropt": (C.c_int, [vp, i32, i32, vp, vp, vp, P(i32), P(i64)]),
         "mlp_solver_set_tour": (C.c_int, [vp, vp, i32]),
         "mlp_solver_set_tour_device": (C.c_int, [vp, vp, i32]),
         "mlp_solver_get_tour": (C.c_int, [vp, vp, i32]),
@@ -368,6 +370,26 @@ class Solver:
                                      C.byref(cnt), C.byref(nc)))
         k = min(cnt.value, max_moves)
         return nc.value, list(zip(ids[:k].tolist(), i[:k].tolist(), j[:k].tolist(), c[:k].tolist()))
+
+    def eval_oropt(self, k: int):
+        """Per-block candidates of Or-opt-k (k in [1, 28])."""
+        m = self.size - k - 2
+        cost = np.zeros(max(m, 0), np.int64)
+        i = np.zeros(max(m, 0), np.int32)
+        j = np.zeros(max(m, 0), np.int32)
+        _check(lib().mlp_solver_eval_oropt(self._h, k, _ptr(cost), _ptr(i), _ptr(j)))
+        return cost, i, j
+
+    def pass_oropt(self, k: int, max_moves: int = 1 << 15):
+        """One Or-opt-k pass; returns (new cost, [(id, i, j, cost)]) with id = k + 1."""
+        i = np.zeros(max_moves, np.int32)
+        j = np.zeros(max_moves, np.int32)
+        c = np.zeros(max_moves, np.int64)
+        cnt, nc = C.c_int32(), C.c_int64()
+        _check(lib().mlp_solver_pass_oropt(self._h, k, max_moves, _ptr(i), _ptr(j), _ptr(c), C.byref(cnt),
+                                           C.byref(nc)))
+        n = min(cnt.value, max_moves)
+        return nc.value, [(k + 1, a, b, d) for a, b, d in zip(i[:n].tolist(), j[:n].tolist(), c[:n].tolist())]
 
     def dvnd(self, nb_mask: int = NB_ALL, max_iters: int = 1 << 20) -> dict:
         st = DvndStats()

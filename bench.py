@@ -649,9 +649,14 @@ def bench_grasp(args, mlpgpu, workloads):
         oracle.random_tour(D, q, 0.5)
     c2 = time.perf_counter()
     t = statistics.median(times)
+    one = []
+    for q in range(5):
+        t0 = time.perf_counter()
+        p.random_tours(seeds[q:q + 1], 0.5)
+        one.append(time.perf_counter() - t0)
     return {"workload": f"{count} starts of MLSolution::random(alpha=0.5) for the n={n} instance, one call "
                         "(seeds from the host, tours copied back)",
-            "seconds": t, "starts_per_s": count / t,
+            "seconds": t, "starts_per_s": count / t, "one_start_ms": statistics.median(one) * 1e3,
             "cpu_oracle_ms_per_start": {"canonical_ties": (c1 - c0) / k * 1e3, "std_sort_ties": (c2 - c1) / k * 1e3,
                                         "sample": f"{k} starts each, 1 thread"}}
 

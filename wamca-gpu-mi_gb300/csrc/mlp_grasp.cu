@@ -11,11 +11,12 @@
 // tour.
 //
 // One warp builds one start.  MT19937 (source/mtrand.cpp:52-124) runs on
-// lane 0 with its state in shared memory; the remaining candidates live in
-// the tail of the tour being built, tour[len..n), and each step selects rank
-// r among them with a three-level radix select (10-bit digits of the 30-bit
-// key distance << 14 | id) over a per-warp 1024-bin histogram, then swaps the
-// selected candidate to tour[len].
+// lane 0 with its state in shared memory.  Each step selects rank r among the
+// remaining candidates with a three-level radix select (10-bit digits of the
+// 30-bit key distance << 14 | id) over a per-warp 1024-bin histogram.  Up to
+// 2048 nodes the candidates and the step's keys stay in shared memory (one
+// distance gather per candidate and step); larger instances keep the
+// candidates in the tail of the tour being built and gather in every pass.
 #include <cmath>
 #include <cstdint>
 
@@ -27,13 +28,16 @@ namespace mlp {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kGraspWarps = 8;  // starts per CTA
+constexpr int kGraspWarps = 8;     // starts per CTA
+constexpr int kGraspSmemN = 2048;  // up to this n a step's keys stay in shared memory
 constexpr int kMtN = 624, kMtM = 397;
 
 struct GraspSmem {
-  static constexpr size_t mt = 0;                              // uint32[kMtN] per warp
-  static constexpr size_t hist = (size_t)kMtN * 4;             // uint32[1024] per warp
-  static constexpr size_t per_warp = hist + 1024 * 4;
+  static constexpr size_t mt = 0;                                 // uint32[kMtN] per warp
+  static constexpr size_t hist = (size_t)kMtN * 4;                // uint32[1024]
+  static constexpr size_t keys = hist + 1024 * 4;                 // uint32[kGraspSmemN]
+  static constexpr size_t ids = keys + (size_t)kGraspSmemN * 4;   // int32[kGraspSmemN]
+  static constexpr size_t per_warp = ids + (size_t)kGraspSmemN * 4;
   static constexpr size_t total = per_warp * kGraspWarps;
 };
 
@@ -83,6 +87,69 @@ __device__ __forceinline__ uint32_t grasp_key(const int32_t* __restrict__ row, i
   return ((uint32_t)row[c] << 14) | (uint32_t)c;
 }
 
+// One step's selection: the key of rank r among the cnt keys key_of(q),
+// q in [0, cnt) (three 10-bit digits, high first).
+template <typename KeyOf>
+__device__ uint32_t select_rank(uint32_t* hist, int cnt, uint32_t r, KeyOf key_of) {
+  const int lane = threadIdx.x & 31;
+  uint32_t prefix = 0;
+#pragma unroll 1
+  for (int lvl = 0; lvl < 3; lvl++) {
+    const int sft = 20 - 10 * lvl;
+    for (int q = lane; q < 1024; q += 32) hist[q] = 0;
+    __syncwarp();
+    for (int q = lane; q < cnt; q += 32) {
+      const uint32_t k = key_of(q);
+      if (lvl == 0 || (k >> (sft + 10)) == prefix) atomicAdd(&hist[(k >> sft) & 1023u], 1u);
+    }
+    __syncwarp();
+    // lane l owns bins 32l .. 32l+31
+    uint32_t own = 0;
+#pragma unroll 8
+    for (int q = 0; q < 32; q++) own += hist[32 * lane + q];
+    uint32_t inc = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += y;
+    }
+    const uint32_t exc = inc - own;
+    const unsigned hit = __ballot_sync(kFull, r >= exc && r < inc);
+    const int src = hit ? __ffs(hit) - 1 : 0;  // the lane whose bins hold rank r
+    uint32_t digit = 0, below = 0;
+    if (lane == src) {
+      uint32_t acc = exc;
+      for (int q = 0; q < 32; q++) {
+        const uint32_t h = hist[32 * lane + q];
+        if (r < acc + h) {
+          digit = 32u * lane + q;
+          below = acc;
+          break;
+        }
+        acc += h;
+      }
+    }
+    digit = __shfl_sync(kFull, digit, src);
+    below = __shfl_sync(kFull, below, src);
+    r -= below;
+    prefix = (prefix << 10) | digit;
+    __syncwarp();  // hist is cleared by the next level
+  }
+  return prefix;
+}
+
+// The position q in [0, cnt) whose key equals `key` (-1 if none).
+template <typename KeyOf>
+__device__ int find_key(int cnt, uint32_t key, KeyOf key_of) {
+  const int lane = threadIdx.x & 31;
+  for (int q0 = 0; q0 < cnt; q0 += 32) {
+    const int q = q0 + lane;
+    const unsigned b = __ballot_sync(kFull, q < cnt && key_of(q) == key);
+    if (b) return q0 + __ffs(b) - 1;
+  }
+  return -1;
+}
+
 __global__ void __launch_bounds__(32 * kGraspWarps)
     k_grasp(const GraspTask* __restrict__ tasks, int count, int* __restrict__ err) {
   extern __shared__ __align__(16) uint8_t gsm[];
@@ -93,13 +160,27 @@ __global__ void __launch_bounds__(32 * kGraspWarps)
   const int32_t* __restrict__ D = task.D;
   const int n = task.n;
   const float alpha = task.alpha;
-  uint32_t* st = (uint32_t*)(gsm + wid * GraspSmem::per_warp + GraspSmem::mt);
-  uint32_t* hist = (uint32_t*)(gsm + wid * GraspSmem::per_warp + GraspSmem::hist);
+  uint8_t* base = gsm + wid * GraspSmem::per_warp;
+  uint32_t* st = (uint32_t*)(base + GraspSmem::mt);
+  uint32_t* hist = (uint32_t*)(base + GraspSmem::hist);
+  uint32_t* keys = (uint32_t*)(base + GraspSmem::keys);
+  int32_t* ids = (int32_t*)(base + GraspSmem::ids);
   int32_t* t = task.tour;
+  // Up to kGraspSmemN nodes the remaining candidates are ids[0..cnt) in
+  // shared memory and their keys are gathered once per step; above, they
+  // are t[len..n) and every pass gathers the keys again.
+  const bool smem = n <= kGraspSmemN;
   int pos = kMtN;
   if (lane == 0) mt_seed(st, task.seed);
-  for (int p = lane; p < n; p += 32) t[p] = p;  // t[0] = depot, candidates 1..n-1 after it
-  if (lane == 0) t[n] = 0;
+  if (smem) {
+    for (int q = lane; q < n - 1; q += 32) ids[q] = q + 1;
+  } else {
+    for (int p = lane; p < n; p += 32) t[p] = p;
+  }
+  if (lane == 0) {
+    t[0] = 0;
+    t[n] = 0;
+  }
   __syncwarp();
   int last = 0;
   for (int len = 1; len < n; len++) {
@@ -112,68 +193,32 @@ __global__ void __launch_bounds__(32 * kGraspWarps)
     r = __shfl_sync(kFull, r, 0);
     if (r >= (uint32_t)cnt) r = cnt - 1;  // alpha <= 1 (checked by the host) keeps r < cnt
     const int32_t* __restrict__ row = D + (size_t)last * n;
-    // rank r among the keys of t[len..n): three 10-bit digits, high first
-    uint32_t prefix = 0;
-#pragma unroll 1
-    for (int lvl = 0; lvl < 3; lvl++) {
-      const int sft = 20 - 10 * lvl;
-      for (int q = lane; q < 1024; q += 32) hist[q] = 0;
+    uint32_t key;
+    int q;
+    if (smem) {
+      for (int x = lane; x < cnt; x += 32) keys[x] = grasp_key(row, ids[x]);
       __syncwarp();
-      for (int p = len + lane; p < n; p += 32) {
-        const uint32_t k = grasp_key(row, t[p]);
-        if (lvl == 0 || (k >> (sft + 10)) == prefix) atomicAdd(&hist[(k >> sft) & 1023u], 1u);
-      }
-      __syncwarp();
-      // lane l owns bins 32l .. 32l+31
-      uint32_t own = 0;
-      for (int q = 0; q < 32; q++) own += hist[32 * lane + q];
-      uint32_t inc = own;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(kFull, inc, o);
-        if (lane >= o) inc += y;
-      }
-      const uint32_t exc = inc - own;
-      const unsigned hit = __ballot_sync(kFull, r >= exc && r < inc);
-      const int src = __ffs(hit) - 1;  // the lane whose bins hold rank r
-      uint32_t digit = 0, below = 0;
-      if (lane == src) {
-        uint32_t acc = exc;
-        for (int q = 0; q < 32; q++) {
-          const uint32_t h = hist[32 * lane + q];
-          if (r < acc + h) {
-            digit = 32u * lane + q;
-            below = acc;
-            break;
-          }
-          acc += h;
-        }
-      }
-      digit = __shfl_sync(kFull, digit, src);
-      below = __shfl_sync(kFull, below, src);
-      r -= below;
-      prefix = (prefix << 10) | digit;
-      __syncwarp();  // hist is cleared by the next level
+      auto key_of = [&](int x) { return keys[x]; };
+      key = select_rank(hist, cnt, r, key_of);
+      q = find_key(cnt, key, key_of);
+    } else {
+      auto key_of = [&](int x) { return grasp_key(row, t[len + x]); };
+      key = select_rank(hist, cnt, r, key_of);
+      q = find_key(cnt, key, key_of);
     }
-    // The selected candidate (keys are distinct: ids are) moves to t[len].
-    int found = -1;
-    for (int p0 = len; p0 < n; p0 += 32) {
-      const int p = p0 + lane;
-      const bool m = p < n && grasp_key(row, t[p]) == prefix;
-      const unsigned b = __ballot_sync(kFull, m);
-      if (b) {
-        found = p0 + __ffs(b) - 1;
-        break;
-      }
-    }
-    const int32_t cur = (int32_t)(prefix & 0x3fffu);
-    if (found < 0) {  // unreachable (the rank-r key exists); t stays a permutation
+    const int32_t cur = (int32_t)(key & 0x3fffu);
+    if (q < 0) {  // unreachable (the rank-r key exists); t stays a permutation
       if (lane == 0) atomicAdd(err, 1);
       return;
     }
     if (lane == 0) {
-      t[found] = t[len];
-      t[len] = cur;
+      if (smem) {
+        ids[q] = ids[cnt - 1];
+        t[len] = cur;
+      } else {
+        t[len + q] = t[len];
+        t[len] = cur;
+      }
     }
     __syncwarp();
     last = cur;

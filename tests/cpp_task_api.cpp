@@ -1,0 +1,95 @@
+// C++ task-API test (include/mlp_gpu.hpp): the reference's own known-answer
+// flow (tests/mlproblem.Test.cpp:11-28, tests/mlsolution.Test.cpp:62-80,
+// tests/WamcaExperiment.Test.cpp:70-131) through the wrappers:
+//   berlin52, distRound = false -> size 53; MTRandom seed 0, random(0.5),
+//   update, ldsUpdate -> cost 494309; one swap kernel pass (launch, GPU merge,
+//   host apply of the merged moves, getSolution, update) -> 367403.
+// Then an Or-opt-5 kernel pass, whose host-applied tour must equal the GPU's,
+// and the device constructor against the host one where no tie decides.
+// Usage: cpp_task_api <berlin52.tsp>; prints "ok" and exits 0 on success.
+#include <cstdio>
+#include <vector>
+
+#include "mlp_gpu.hpp"
+
+using namespace wamca;
+
+#define EXPECT(c)                                                   \
+  do {                                                              \
+    if (!(c)) {                                                     \
+      std::printf("FAILED %s (line %d)\n", #c, __LINE__);           \
+      return 1;                                                     \
+    }                                                               \
+  } while (0)
+
+static int run_pass(MLKernel& kernel, MLSolution& sol) {
+  kernel.setSolution(&sol);
+  kernel.sendSolution();
+  kernel.defineKernelGrid();
+  kernel.launchKernel();
+  kernel.sync();
+  kernel.mergeGPU();
+  kernel.recvResult();
+  int applied = 0;
+  for (uint32_t q = 0; q < kernel.moveElems; q++) {
+    if (kernel.moveData[q].cost < 0) {
+      kernel.applyMove(kernel.moveData[q]);
+      applied++;
+    }
+  }
+  kernel.getSolution(&sol);
+  sol.update();
+  return applied;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 2) return 2;
+  try {
+    MLProblem problem(true, false, false);
+    problem.load(argv[1]);
+    EXPECT(problem.size == 53);  // K2
+
+    MTRandom rng;
+    rng.seed(0);
+    MLSolution sol(problem);
+    sol.random(rng, 0.50f);
+    sol.update();
+    sol.ldsUpdate();
+    EXPECT(sol.costCalc() == 494309u);  // K3
+    EXPECT(sol.adsData()[3] == 494309u);  // the ADS header carries the cost (mlads.h:38-74)
+
+    MLKernelSwap swap(problem);
+    swap.init(true);
+    EXPECT(swap.moveElems == 0);
+    const int applied = run_pass(swap, sol);
+    EXPECT(applied == 6);
+    sol.ldsUpdate();
+    EXPECT(sol.costCalc() == 367403u);  // K4
+    swap.term();
+
+    // Or-opt-5 (a kernel the reference allocates but never runs): the host
+    // apply of the merged moves reproduces the GPU's tour.
+    MLKernelOrOpt oropt5(problem, 5);
+    oropt5.init(true);
+    const uint32_t before = sol.cost;
+    run_pass(oropt5, sol);
+    EXPECT(oropt5.moveElems == oropt5.moveData.size());
+    std::vector<int32_t> gpu(problem.size);
+    check(mlp_solver_get_tour(oropt5.handle(), gpu.data(), (int32_t)gpu.size()));
+    EXPECT(gpu == sol.tour());
+    EXPECT(sol.cost <= before);
+
+    // The device constructor equals the host one when no tie decides a pick.
+    MTRandom r2;
+    r2.seed(0);
+    MLSolution host(problem), dev(problem);
+    host.random(r2, 0.90f);
+    dev.randomDevice(0, 0.90f);
+    EXPECT(host.tour() == dev.tour() && host.cost == dev.cost);
+  } catch (const std::exception& e) {
+    std::printf("exception: %s\n", e.what());
+    return 1;
+  }
+  std::printf("ok\n");
+  return 0;
+}

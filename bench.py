@@ -27,6 +27,8 @@ Beside the headline, in the same line:
   grasp      the multi-start constructor (MLSolution::random) on the device:
              2048 starts at n = 1000, beside the oracle's CPU time per start
   oropt_k    Or-opt-k for k = 4, 8, 16, 28 at n = 1000: candidates and a pass
+  reference_gpu  the reference's own neighbourhood kernels (compiled from its
+             sources for sm_103a) on the same GPU, beside the fused sweep
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -695,6 +697,49 @@ def bench_oropt_k(args, mlpgpu, workloads, stream):
             **out}
 
 
+def bench_reference_gpu(args, mlpgpu, workloads, stream, flush):
+    """The reference's own ODC neighbourhood kernels (compiled from its sources
+    for sm_103a into oracle/_ref/*.cubin, launched with its own grid, block and
+    shared-memory configuration) on this GPU for the n = 1000 instance, beside
+    the engine's fused sweep of the same five neighbourhoods."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the reference-kernel launcher (baseline leg)
+
+    try:
+        L = oracle.ref_gpu()
+    except RuntimeError as e:
+        return {"unavailable": str(e)}
+    if L is None:
+        return {"unavailable": "reference kernels not built (its sources were absent when this tree was prepared)"}
+    n = N_NODES
+    size = n + 1
+    x, y = workloads.uniform_instance(n, INSTANCE_SEED)
+    s = mlpgpu.Solver(mlpgpu.Problem.from_coords(x, y, dist_round=True))
+    s.set_stream(stream.cuda_stream)
+    s.set_tour(workloads.random_perm_tour(n, 7))
+    ads = np.zeros(32 + size * (size + 3), np.uint32)
+    mlpgpu._check(mlpgpu.lib().mlp_solver_ads(s._h, mlpgpu._ptr(ads), len(ads)))
+    ads_dev = torch.from_numpy(ads.view(np.int32)).cuda()
+    moves = torch.zeros(size, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    names = ["swap", "2opt", "oropt1", "oropt2", "oropt3"]
+    kernels, total_ms = {}, 0.0
+    for nb, nm in enumerate(names):
+        oracle.ref_gpu_eval(nb, ads_dev.data_ptr(), size, moves.data_ptr(), 3)
+        ms, block, grid = oracle.ref_gpu_eval(nb, ads_dev.data_ptr(), size, moves.data_ptr(), 20)
+        kernels[nm] = {"ms": ms, "block": block, "grid": grid}
+        total_ms += ms
+    t_ours = time_sweep(mlpgpu, s, stream, flush, mlpgpu.NB_ALL, 20)
+    return {"workload": f"n={n}: the reference's kernelSwap / kernel2Opt / kernelOrOpt(k=1,2,3) on this GPU, "
+                        "its own launch configuration, mean of 20 back-to-back launches each (inputs L2-resident)",
+            "kernels": kernels, "reference_sum_ms": total_ms, "ours_fused_sweep_ms": t_ours * 1e3,
+            "speedup": total_ms / (t_ours * 1e3),
+            "note": "the engine's sweep is timed cold-L2 (flushed before every launch); the reference kernels read "
+                    "8 KB of coordinates and weights and compute distances from coordinates (+0 rounding)"}
+
+
 def run_ours(args, world, rank, local) -> None:
     import torch
 
@@ -717,7 +762,8 @@ def run_ours(args, world, rank, local) -> None:
               "large": lambda: bench_large(args, mlpgpu, workloads, stream, flush),
               "total": lambda: bench_total(args, mlpgpu, workloads, stream, flush),
               "grasp": lambda: bench_grasp(args, mlpgpu, workloads),
-              "oropt_k": lambda: bench_oropt_k(args, mlpgpu, workloads, stream)}[args.only]
+              "oropt_k": lambda: bench_oropt_k(args, mlpgpu, workloads, stream),
+              "reference_gpu": lambda: bench_reference_gpu(args, mlpgpu, workloads, stream, flush)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}))
         return
@@ -744,6 +790,8 @@ def run_ours(args, world, rank, local) -> None:
             extra["grasp"] = bench_grasp(args, mlpgpu, workloads)
         if "oropt_k" in wl:
             extra["oropt_k"] = bench_oropt_k(args, mlpgpu, workloads, stream)
+        if "reference_gpu" in wl:
+            extra["reference_gpu"] = bench_reference_gpu(args, mlpgpu, workloads, stream, flush)
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -799,7 +847,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-iters", type=int, default=1 << 20)
-    ap.add_argument("--workloads", default="batched,serving,large,total,grasp,oropt_k",
+    ap.add_argument("--workloads", default="batched,serving,large,total,grasp,oropt_k,reference_gpu",
                     help="extra workloads reported beside the plain n=1000 headline")
     ap.add_argument("--batch-instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=128)
@@ -812,7 +860,8 @@ def main() -> None:
     ap.add_argument("--total-reps", type=int, default=5)
     ap.add_argument("--grasp-starts", type=int, default=2048)
     ap.add_argument("--total-cpu-iters", type=int, default=8)
-    ap.add_argument("--only", choices=["batched", "serving", "large", "total", "grasp", "oropt_k"], default=None,
+    ap.add_argument("--only", choices=["batched", "serving", "large", "total", "grasp", "oropt_k", "reference_gpu"],
+                    default=None,
                     help="run one extra workload alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -28,14 +28,62 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+REF_DIR = os.path.join(HERE, "_ref")
+REF_CUBINS = [os.path.join(REF_DIR, f"ref_{u}.cubin") for u in ("mlkswap", "mlk2opt", "mlkoropt")]
+REF_LAUNCH = os.path.join(REF_DIR, "libref_launch.so")
+
+
 def build_ref() -> Optional[str]:
-    """Compiles the reference's CPU evaluator into _ref/ (only where the
-    reference sources are mounted); returns the library path or None."""
+    """Compiles the reference's CPU evaluator and its GPU neighbourhood kernels
+    (sm_103a cubins) into _ref/ where the reference sources are mounted, and
+    the launcher of those kernels wherever the cubins are (they travel with
+    the tree); returns the CPU evaluator's path or None."""
     ref_src = os.environ.get("REF_SRC", "/root/reference/source")
-    if not os.path.isdir(ref_src):
-        return REF_LIB if os.path.exists(REF_LIB) else None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
-    return REF_LIB
+    if os.path.isdir(ref_src):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "refgpu", f"REF_SRC={ref_src}"], check=True)
+    if all(os.path.exists(c) for c in REF_CUBINS):
+        subprocess.run(["make", "-s", "-C", HERE, "reflaunch"], check=True)
+    return REF_LIB if os.path.exists(REF_LIB) else None
+
+
+_ref_gpu: Optional[C.CDLL] = None
+
+
+def ref_gpu() -> Optional[C.CDLL]:
+    """The launcher of the reference's own GPU kernels (oracle/ref_launch.cpp),
+    initialised on the current device; None where they were not built."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        if not (os.path.exists(REF_LAUNCH) and all(os.path.exists(c) for c in REF_CUBINS)):
+            return None
+        L = C.CDLL(REF_LAUNCH)
+        L.rl_error.restype = C.c_char_p
+        L.rl_init.argtypes = [C.c_char_p]
+        L.rl_eval.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_uint64, C.c_int, C.POINTER(C.c_float),
+                              C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        if L.rl_init(REF_DIR.encode()) != 0:
+            raise RuntimeError("reference kernels: " + L.rl_error().decode())
+        _ref_gpu = L
+    return _ref_gpu
+
+
+def ref_gpu_eval(nb: int, ads_dev: int, size: int, moves_dev: int, reps: int = 1):
+    """Runs the reference's ODC kernel of nb (0 swap, 1 2-opt, 2..4 Or-opt-1..3)
+    over the device MLADSData buffer; returns (ms per launch, block, grid)."""
+    L = ref_gpu()
+    ms, blk, grd = C.c_float(), C.c_int(), C.c_int()
+    if L.rl_eval(nb, ads_dev, size, moves_dev, reps, C.byref(ms), C.byref(blk), C.byref(grd)) != 0:
+        raise RuntimeError("reference kernel: " + L.rl_error().decode())
+    return ms.value, blk.value, grd.value
+
+
+def decode_move_pack(w: np.ndarray):
+    """MLMovePack words (source/mlads.h:180-215): (cost, id, i, j)."""
+    w = np.asarray(w, dtype=np.uint64)
+    cost = (w >> np.uint64(32)).astype(np.uint32).view(np.int32).astype(np.int64)
+    low = (w & np.uint64(0xffffffff)).astype(np.uint32)
+    return cost, (low & 0xF).astype(np.int32), ((low >> 4) & 0x3FFF).astype(np.int32), (low >> 18).astype(np.int32)
 
 
 def lib() -> C.CDLL:

@@ -710,7 +710,7 @@ int JobSet::set_total(bool on) {
              "copy jobs");
     MLP_CUDA(cudaStreamSynchronize(stream_), "copy jobs");
     shape_user_ = shape_;
-    shape_ = kTotalShape;
+    shape_ = total_shape(max_size_);
   } else {
     shape_ = shape_user_;
   }
@@ -721,7 +721,7 @@ int JobSet::set_total(bool on) {
 int JobSet::launch_iteration() {
   if (total_) {
     const int nj = (int)jobs_.size();
-    MLP_CUDA(launch_sweep_collect(dtiles_, ntiles_, djobs_, wide_, stream_), "sweep kernel");
+    MLP_CUDA(launch_sweep_collect(dtiles_, ntiles_, djobs_, wide_, shape_, stream_), "sweep kernel");
     MLP_CUDA(launch_total_select(djobs_, nj, wide_, stream_), "TOTAL greedy kernel");
     MLP_CUDA(launch_total_finish(djobs_, nj, wide_, solo_smem_, max_size_, stream_), "merge kernel");
     return kOk;

@@ -1542,12 +1542,18 @@ cudaError_t launch_sweep(const SweepTile* tiles, int ntiles, const JobDev* jobs,
               : sweep_dispatch<false>(tiles, ntiles, jobs, shape, io, s);
 }
 
-cudaError_t launch_sweep_collect(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
+cudaError_t launch_sweep_collect(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide, int shape,
                                  cudaStream_t s) {
   if (ntiles <= 0) return cudaSuccess;
-  static_assert(kTileShapes[kTotalShape].tl == 32 && kTileShapes[kTotalShape].tr == 16, "collect tile shape");
-  return wide ? sweep_collect_launch<true, 32, 16>(tiles, ntiles, jobs, s)
-              : sweep_collect_launch<false, 32, 16>(tiles, ntiles, jobs, s);
+  static_assert(kTileShapes[kTotalShapeSmall].tl == 64 && kTileShapes[kTotalShapeSmall].tr == 4, "collect shape");
+  static_assert(kTileShapes[kTotalShapeLarge].tl == 128 && kTileShapes[kTotalShapeLarge].tr == 16, "collect shape");
+  if (shape == kTotalShapeSmall)
+    return wide ? sweep_collect_launch<true, 64, 4>(tiles, ntiles, jobs, s)
+                : sweep_collect_launch<false, 64, 4>(tiles, ntiles, jobs, s);
+  if (shape == kTotalShapeLarge)
+    return wide ? sweep_collect_launch<true, 128, 16>(tiles, ntiles, jobs, s)
+                : sweep_collect_launch<false, 128, 16>(tiles, ntiles, jobs, s);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,

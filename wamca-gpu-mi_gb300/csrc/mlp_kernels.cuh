@@ -58,11 +58,13 @@ cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use
                               cudaStream_t s);
 // TOTAL candidate mode (every evaluated move is a merge candidate).
 // The collecting sweep appends each job's improving moves to its TOTAL lists
-// (tile shape kTotalShape); the TOTAL greedy selects per neighbourhood
-// (mlp_total.cu); the finish runs the cross-neighbourhood greedy, apply and
-// ADS rebuild (one CTA per job, the k_merge_solo workspace).
-constexpr int kTotalShape = 2;  // 32 diagonals x 16 rows
-cudaError_t launch_sweep_collect(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide,
+// (compiled for the tile shapes total_shape() picks); the TOTAL greedy selects
+// per neighbourhood (mlp_total.cu); the finish runs the cross-neighbourhood
+// greedy, apply and ADS rebuild (one CTA per job, the k_merge_solo workspace).
+constexpr int kTotalShapeSmall = 3;  // 64 diagonals x 4 rows: sets whose tours have <= 2000 positions
+constexpr int kTotalShapeLarge = 7;  // 128 diagonals x 16 rows
+inline int total_shape(int max_size) { return max_size <= 2000 ? kTotalShapeSmall : kTotalShapeLarge; }
+cudaError_t launch_sweep_collect(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide, int shape,
                                  cudaStream_t s);
 cudaError_t launch_total_select(const JobDev* jobs, int njobs, bool wide, cudaStream_t s);
 cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,

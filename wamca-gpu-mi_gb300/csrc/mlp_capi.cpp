@@ -259,12 +259,15 @@ MLP_API int mlp_problem_random_tours(mlp_problem_t h, int32_t count, const uint3
     cudaStream_t st = nullptr;
     int32_t* d = nullptr;
     ~Res() {
-      if (d) cudaFree(d);
-      if (st) cudaStreamDestroy(st);
+      if (d) cudaFreeAsync(d, st);
+      if (st) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+      }
     }
   } r;
   MLP_CUDA(cudaStreamCreateWithFlags(&r.st, cudaStreamNonBlocking), "stream");
-  MLP_CUDA(cudaMalloc(&r.d, sizeof(int32_t) * sz * (size_t)count), "cudaMalloc(tours)");
+  MLP_CUDA(cudaMallocAsync(&r.d, sizeof(int32_t) * sz * (size_t)count, r.st), "cudaMallocAsync(tours)");
   std::vector<GraspTask> tasks;
   for (int32_t q = 0; q < count; q++) tasks.push_back(GraspTask{p->dD, r.d + q * sz, p->n, seeds[q], alpha, 0});
   MLP_TRY(build_random_tours(tasks, r.st));
@@ -485,16 +488,17 @@ MLP_API int mlp_solver_pass_oropt(mlp_solver_t s, int32_t k, int32_t max_moves, 
   MLP_TRY(oropt_k_check(s, k));
   if (max_moves > 0 && (!is || !js || !costs)) return arg_error("null move arrays");
   const int sz = s->prob->size, m = oropt_blocks(k, sz);
-  struct Scratch {
+  struct Scratch {  // stream-ordered: no device-wide synchronisation
+    cudaStream_t st;
     uint8_t* p = nullptr;
     ~Scratch() {
-      if (p) cudaFree(p);
+      if (p) cudaFreeAsync(p, st);
     }
-  } sc;
+  } sc{s->set->stream()};
   const size_t body = oropt_pass_scratch_bytes(sz, k);
   const size_t o_ij = (body + 255) / 256 * 256, o_cost = o_ij + ((size_t)m * 4 + 255) / 256 * 256;
   const size_t o_cnt = o_cost + (size_t)m * 8, bytes = o_cnt + 256;
-  MLP_CUDA(cudaMalloc(&sc.p, bytes), "cudaMalloc(Or-opt-k pass)");
+  MLP_CUDA(cudaMallocAsync(&sc.p, bytes, s->set->stream()), "cudaMallocAsync(Or-opt-k pass)");
   MLP_TRY(oropt_eval_keys(s, k));
   uint32_t* dij = (uint32_t*)(sc.p + o_ij);
   int64_t* dcost = (int64_t*)(sc.p + o_cost);

@@ -476,21 +476,22 @@ int check_alpha(float alpha) {
 
 int build_random_tours(const std::vector<GraspTask>& tasks, cudaStream_t stream) {
   if (tasks.empty()) return kOk;
-  struct Buffers {
+  struct Buffers {  // stream-ordered: no device-wide synchronisation
+    cudaStream_t st;
     GraspTask* tasks = nullptr;
     int* err = nullptr;
     ~Buffers() {
-      if (tasks) cudaFree(tasks);
-      if (err) cudaFree(err);
+      if (tasks) cudaFreeAsync(tasks, st);
+      if (err) cudaFreeAsync(err, st);
     }
-  } b;
+  } b{stream};
   for (const GraspTask& t : tasks)
     if (t.n < 1 || t.n > kMaxSize - 1 || !t.D || !t.tour) {
       set_error("constructor task out of range");
       return kErrArg;
     }
-  MLP_CUDA(cudaMalloc(&b.tasks, sizeof(GraspTask) * tasks.size()), "cudaMalloc(constructor tasks)");
-  MLP_CUDA(cudaMalloc(&b.err, sizeof(int)), "cudaMalloc(constructor flag)");
+  MLP_CUDA(cudaMallocAsync(&b.tasks, sizeof(GraspTask) * tasks.size(), stream), "cudaMallocAsync(constructor tasks)");
+  MLP_CUDA(cudaMallocAsync(&b.err, sizeof(int), stream), "cudaMallocAsync(constructor flag)");
   MLP_CUDA(cudaMemcpyAsync(b.tasks, tasks.data(), sizeof(GraspTask) * tasks.size(), cudaMemcpyHostToDevice,
                            stream),
            "copy constructor tasks");

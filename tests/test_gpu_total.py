@@ -80,3 +80,15 @@ def test_total_batch_equals_alone(mlpgpu_mod):
         bt, bst = b.result(q)
         assert np.array_equal(bt, ot), q
         assert bst["cost"] == ost["cost"] and bst["moves"] == ost["moves"], q
+
+
+@pytest.mark.parametrize("wide,nbs,iters", [(False, [0, 1], 2), (True, [1, 4], 1)])
+def test_total_large_size_global_workspace(mlpgpu_mod, wide, nbs, iters):
+    # n = 2500: the finish runs from the job's global merge workspace (the
+    # stage-3 list no longer fits shared memory), the lists hold millions of keys.
+    s, t, D = _setup(mlpgpu_mod, 2500, 9, wide=wide)
+    mask = sum(1 << nb for nb in nbs)
+    st = s.dvnd(mask, iters)
+    ot, ost = oracle.dvnd_total(t, D, wide, nbs=nbs, max_iters=iters)
+    assert np.array_equal(s.tour(), ot)
+    assert st["cost"] == ost["cost"] and st["moves"] == ost["moves"]

@@ -219,6 +219,28 @@ def cpu_baseline(size_n: int, budget_s: float = 12.0) -> dict:
                       f"instance, {sweep_evals(size_n + 1)} evals each, oracle with {cores} OpenMP threads"}
 
 
+def cpu_solves_sample(items, max_n: int = 1 << 30) -> dict:
+    """The oracle's DVND on a bounded sample of searches, one search per host
+    thread (ctypes releases the GIL), all host threads: the CPU baseline of
+    the many-search forms.  items: (x, y, start tour) of the sampled searches;
+    searches with n > max_n are left out of the sample."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    work = [(oracle.dist(x, y, True), t) for x, y, t in items if len(x) <= max_n]
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(lambda a: oracle.dvnd(a[1], a[0], threads=1), work))
+    dt = time.perf_counter() - t0
+    ns = [D.shape[0] for D, _ in work]
+    return {"solves_per_s": len(work) / dt, "seconds": dt, "searches": len(work), "cores": cores,
+            "mean_n": statistics.mean(ns) if ns else 0, "kind": "port",
+            "sample": f"{len(work)} searches of the workload, oracle DVND, one per host thread"}
+
+
 def run_reference(args, world, rank) -> None:
     """Reference arm: the reference path's CPU restatement (oracle port) timed on
     the host cores -- full DVND solves of the same workload, all host threads."""
@@ -429,6 +451,9 @@ def bench_batched(args, mlpgpu, workloads, stream):
         assert st["cost"] == res[j]["cost"] and st["sweeps"] == res[j]["sweeps"], "batched and plain differ"
     plain_solves = len(sample) / t_plain
     batched_solves = len(searches) / t_batch
+    csample = list(range(0, len(searches), max(1, len(searches) // args.cpu_sample)))
+    cpu = cpu_solves_sample([(workloads.clustered_instance(int(sizes[searches[j][0]]), 40_000 + searches[j][0]) +
+                              (searches[j][1],)) for j in csample]) if not args.no_cpu else None
     return {
         "workload": f"{ninst} instances x {starts} starts = {len(searches)} DVND searches, n log-uniform "
                     "[100,1000], 8-cluster coordinates (sigma 50), one batch",
@@ -438,6 +463,7 @@ def bench_batched(args, mlpgpu, workloads, stream):
         "plain_solves_per_s": plain_solves, "plain_sample": len(sample),
         "speedup_vs_plain": batched_solves / plain_solves,
         "results_equal_plain": True,
+        "cpu_baseline": cpu,
     }
 
 
@@ -508,6 +534,10 @@ def bench_serving(args, mlpgpu, workloads):
         p.close()
     out["plain_solves_per_s"] = cnt / t_plain
     out["plain_sample"] = cnt
+    if not args.no_cpu:
+        k = max(1, nreq // args.cpu_sample)
+        out["cpu_baseline"] = cpu_solves_sample([reqs[j] for j in range(0, nreq, k)], max_n=1000)
+        out["cpu_baseline"]["sample"] += " (requests with n <= 1000 of every k-th request)"
     return out
 
 
@@ -846,6 +876,8 @@ def main() -> None:
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--cpu-sample", type=int, default=32,
+                    help="searches sampled for the CPU baseline of the batched and serving forms")
     ap.add_argument("--ref-iters", type=int, default=1 << 20)
     ap.add_argument("--workloads", default="batched,serving,large,total,grasp,oropt_k,reference_gpu",
                     help="extra workloads reported beside the plain n=1000 headline")

@@ -231,6 +231,7 @@ MLP_API int mlp_solver_set_total(mlp_solver_t s, int32_t on) {
 }
 
 MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len) {
+  MLP_RANGE("mlp_solver_set_tour");
   if (!s) return arg_error("null solver");
   MLP_TRY(validate_tour(tour, len, s->prob->n, s->prob->size));
   MLP_CUDA(cudaMemcpyAsync(s->job->dev.tour, tour, sizeof(int32_t) * len, cudaMemcpyHostToDevice,
@@ -240,6 +241,7 @@ MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len
 }
 
 MLP_API int mlp_solver_random_tour(mlp_solver_t s, uint32_t seed, float alpha) {
+  MLP_RANGE("mlp_solver_random_tour");
   if (!s) return arg_error("null solver");
   MLP_TRY(check_alpha(alpha));
   const std::vector<GraspTask> task{GraspTask{s->prob->dD, s->job->dev.tour, s->prob->n, seed, alpha, 0}};
@@ -249,6 +251,7 @@ MLP_API int mlp_solver_random_tour(mlp_solver_t s, uint32_t seed, float alpha) {
 
 MLP_API int mlp_problem_random_tours(mlp_problem_t h, int32_t count, const uint32_t* seeds, float alpha,
                                      int32_t* tours) {
+  MLP_RANGE("mlp_problem_random_tours");
   Problem* p = reinterpret_cast<Problem*>(h);
   if (!p) return arg_error("null problem");
   if (count < 0 || (count > 0 && (!seeds || !tours))) return arg_error("count must be >= 0 with seeds and tours");
@@ -377,6 +380,7 @@ MLP_API int mlp_solver_weights(mlp_solver_t s, int32_t* w, int32_t len) {
 }
 
 MLP_API int mlp_solver_ads(mlp_solver_t s, uint32_t* ads, int64_t words) {
+  MLP_RANGE("mlp_solver_ads");
   if (!s || !ads) return arg_error("null argument");
   const int sz = s->prob->size;
   const size_t need = 32 + (size_t)sz * (sz + 3);
@@ -411,6 +415,7 @@ MLP_API int mlp_solver_num_candidates(mlp_solver_t s, int32_t nb, int32_t* count
 }
 
 MLP_API int mlp_solver_eval(mlp_solver_t s, int32_t nb, int64_t* cost, int32_t* oi, int32_t* oj) {
+  MLP_RANGE("mlp_solver_eval");
   if (!s || !cost || !oi || !oj) return arg_error("null argument");
   if (nb < 0 || nb >= kNumNb) return arg_error("neighbourhood out of range");
   const int sz = s->prob->size;
@@ -457,6 +462,7 @@ static int oropt_eval_keys(mlp_solver_t s, int32_t k) {
 }
 
 MLP_API int mlp_solver_eval_oropt(mlp_solver_t s, int32_t k, int64_t* cost, int32_t* oi, int32_t* oj) {
+  MLP_RANGE("mlp_solver_eval_oropt");
   MLP_TRY(oropt_k_check(s, k));
   if (!cost || !oi || !oj) return arg_error("null argument");
   const int sz = s->prob->size, m = oropt_blocks(k, sz);
@@ -485,6 +491,7 @@ MLP_API int mlp_solver_eval_oropt(mlp_solver_t s, int32_t k, int64_t* cost, int3
 
 MLP_API int mlp_solver_pass_oropt(mlp_solver_t s, int32_t k, int32_t max_moves, int32_t* is, int32_t* js,
                                   int64_t* costs, int32_t* count, int64_t* new_cost) {
+  MLP_RANGE("mlp_solver_pass_oropt");
   MLP_TRY(oropt_k_check(s, k));
   if (max_moves > 0 && (!is || !js || !costs)) return arg_error("null move arrays");
   const int sz = s->prob->size, m = oropt_blocks(k, sz);
@@ -528,6 +535,7 @@ MLP_API int mlp_solver_pass_oropt(mlp_solver_t s, int32_t k, int32_t max_moves, 
 
 MLP_API int mlp_solver_pass(mlp_solver_t s, int32_t nb, int32_t max_moves, int32_t* ids, int32_t* is,
                             int32_t* js, int64_t* costs, int32_t* count, int64_t* new_cost) {
+  MLP_RANGE("mlp_solver_pass");
   if (!s) return arg_error("null solver");
   if (nb < 0 || nb >= kNumNb) return arg_error("neighbourhood out of range");
   if (max_moves > 0 && (!ids || !is || !js || !costs)) return arg_error("null move arrays");
@@ -565,6 +573,7 @@ MLP_API int mlp_solver_pass(mlp_solver_t s, int32_t nb, int32_t max_moves, int32
 }
 
 MLP_API int mlp_solver_dvnd(mlp_solver_t s, int32_t nb_mask, int32_t max_iters, mlp_dvnd_stats_t* stats) {
+  MLP_RANGE("mlp_solver_dvnd");
   if (!s) return arg_error("null solver");
   MLP_TRY(s->set->set_mask(nb_mask));
   MLP_TRY(s->set->run(max_iters, true));
@@ -572,6 +581,7 @@ MLP_API int mlp_solver_dvnd(mlp_solver_t s, int32_t nb_mask, int32_t max_iters, 
 }
 
 MLP_API int mlp_solver_dvnd_async(mlp_solver_t s, int32_t nb_mask, int32_t max_iters) {
+  MLP_RANGE("mlp_solver_dvnd_async");
   if (!s) return arg_error("null solver");
   MLP_TRY(s->set->set_mask(nb_mask));
   return s->set->enqueue_device_loop(max_iters);
@@ -586,6 +596,7 @@ MLP_API int mlp_solver_begin(mlp_solver_t s, int32_t nb_mask, int32_t max_iters)
 }
 
 MLP_API int mlp_solver_enqueue(mlp_solver_t s, int32_t iterations) {
+  MLP_RANGE("mlp_solver_enqueue");
   if (!s) return arg_error("null solver");
   if (iterations <= 0) return arg_error("iterations must be positive");
   return s->set->enqueue_iterations(iterations);
@@ -597,6 +608,7 @@ MLP_API int mlp_solver_stats(mlp_solver_t s, mlp_dvnd_stats_t* stats) {
 }
 
 MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats, int64_t* evals_per_sweep) {
+  MLP_RANGE("mlp_solver_sweep");
   if (!s) return arg_error("null solver");
   if (repeats < 0) return arg_error("repeats must be >= 0");
   MLP_TRY(s->set->set_mask(nb_mask));
@@ -787,6 +799,7 @@ MLP_API int mlp_batch_reset(mlp_batch_t b) {
 }
 
 MLP_API int mlp_batch_run(mlp_batch_t b, int32_t nb_mask, int32_t max_iters) {
+  MLP_RANGE("mlp_batch_run");
   if (!b) return arg_error("null batch");
   MLP_TRY(batch_build(b));
   MLP_TRY(b->set->set_mask(nb_mask));
@@ -795,6 +808,7 @@ MLP_API int mlp_batch_run(mlp_batch_t b, int32_t nb_mask, int32_t max_iters) {
 }
 
 MLP_API int mlp_batch_run_async(mlp_batch_t b, int32_t nb_mask, int32_t max_iters) {
+  MLP_RANGE("mlp_batch_run_async");
   if (!b) return arg_error("null batch");
   MLP_TRY(batch_build(b));
   MLP_TRY(b->set->set_mask(nb_mask));

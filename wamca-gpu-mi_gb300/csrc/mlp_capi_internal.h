@@ -6,7 +6,19 @@
 #include <memory>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "mlp_engine.h"
+
+// NVTX range around a public entry point (Nsight Systems / Compute show the
+// library's calls by name; a no-op without a tool attached).
+struct MlpRange {
+  explicit MlpRange(const char* name) { nvtxRangePushA(name); }
+  ~MlpRange() { nvtxRangePop(); }
+  MlpRange(const MlpRange&) = delete;
+  MlpRange& operator=(const MlpRange&) = delete;
+};
+#define MLP_RANGE(name) MlpRange mlp_range_(name)
 
 struct mlp_solver {
   mlp::Problem* prob = nullptr;

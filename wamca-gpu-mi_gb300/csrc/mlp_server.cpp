@@ -451,6 +451,7 @@ MLP_API int mlp_server_set_tile_shape(mlp_server_t s, int32_t shape) {
 MLP_API int mlp_server_submit(mlp_server_t s, int32_t n, const int32_t* x, const int32_t* y, int32_t dist_round,
                               const int32_t* tour, int32_t len, int32_t nb_mask, int32_t max_iters,
                               double arrival, int64_t* id) {
+  MLP_RANGE("mlp_server_submit");
   if (!s || !x || !y || !tour) return arg_error("null argument");
   if (n < 5 || n + 1 > kMaxSize) {
     set_error("n must lie in [5, max size - 1]");
@@ -488,6 +489,7 @@ MLP_API int mlp_server_submit(mlp_server_t s, int32_t n, const int32_t* x, const
 }
 
 MLP_API int mlp_server_step(mlp_server_t s, int32_t iters, int32_t* active, int32_t* queued) {
+  MLP_RANGE("mlp_server_step");
   if (!s) return arg_error("null server");
   if (iters < 0 || iters > 4096) return arg_error("iters must lie in [0, 4096]");
   const int st = server_step(s, iters);

@@ -92,3 +92,17 @@ def test_total_large_size_global_workspace(mlpgpu_mod, wide, nbs, iters):
     ot, ost = oracle.dvnd_total(t, D, wide, nbs=nbs, max_iters=iters)
     assert np.array_equal(s.tour(), ot)
     assert st["cost"] == ost["cost"] and st["moves"] == ost["moves"]
+
+
+def test_total_dvnd_device_loop_and_async(mlpgpu_mod):
+    # The three TOTAL kernels captured in the CUDA graph's conditional while
+    # node (set_unroll(0)) and the enqueued form give the host loop's result.
+    s, t, D = _setup(mlpgpu_mod, 180, 12)
+    ot, ost = oracle.dvnd_total(t, D)
+    s.set_unroll(0)
+    st = s.dvnd()
+    assert np.array_equal(s.tour(), ot) and st["cost"] == ost["cost"] and st["converged"] == 1
+    s.set_tour(t)
+    s.dvnd_async()
+    st2 = s.stats()
+    assert np.array_equal(s.tour(), ot) and st2["cost"] == ost["cost"]

@@ -514,6 +514,7 @@ struct __align__(16) Rec {
   uint32_t st;   // kNone / kUndec / kIn / kOut
 };
 constexpr int kBitMax = 512;         // stage-3 conflict bit-matrix capacity (moves)
+constexpr int kBitMaxWs = 4096;      // the same in a global merge workspace (large tours: 2 MB)
 constexpr int kMergeThreads = 1024;
 constexpr int kClusterCtas = 6;  // five stage-2 CTAs and the stage-3 leader
 
@@ -553,6 +554,12 @@ struct MergeLayout {
     total = align_up(s2 > s3 ? s2 : s3, 128);
   }
 };
+
+// A global merge workspace holds the cluster's (or the one-CTA) layout and,
+// when a job's stage-3 list can exceed kBitMax moves, a kBitMaxWs-move
+// conflict bit matrix after it.
+__host__ __device__ size_t ws_big_bits_offset(int size);
+__host__ __device__ __forceinline__ size_t ws_big_bits_bytes() { return (size_t)kBitMaxWs * (kBitMaxWs / 32) * 4; }
 
 __device__ __forceinline__ void amin(uint64_t* p, uint64_t v) {
   atomicMin((unsigned long long*)p, (unsigned long long)v);
@@ -754,19 +761,21 @@ __device__ __forceinline__ int id_of(uint64_t key3) { return (int)((key3 >> kCtx
 // rebuild and the candidate-key reset, by one whole CTA on the list
 // key3 / shp3 / ij3 / st3[0, m3) of kept stage-2 moves (any order; every
 // st3 entry kUndec).  t_old holds the current tour; bits, owner and t_new are
-// workspace (bits: min(m3, kBitMax)^2 bits).
+// workspace (bits: min(m3, kBitMax)^2 bits); bits_big (may be null) holds
+// kBitMaxWs^2 bits for lists longer than kBitMax (global merge workspaces).
 template <bool WIDE>
 __device__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* key3, const uint64_t* shp3,
                              const uint32_t* ij3, volatile uint8_t* st3, uint32_t* bits, int32_t* owner,
-                             int32_t* t_old, int32_t* t_new) {
-  __shared__ uint32_t s_in[kBitMax / 32], s_und[kBitMax / 32];
+                             int32_t* t_old, int32_t* t_new, uint32_t* bits_big = nullptr) {
+  __shared__ uint32_t s_in[kBitMaxWs / 32], s_und[kBitMaxWs / 32];
   __shared__ int s_ns;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
   int32_t* tour = J->tour;
   if (tid == 0) s_ns = 0;
   __syncthreads();
-  if (m3 <= kBitMax) {
+  if (m3 > kBitMax) bits = m3 <= kBitMaxWs ? bits_big : nullptr;
+  if (bits != nullptr) {
     // conflict rows: bit y of row x <=> y precedes x and !canMerge(y, x)
     const int W3 = (m3 + 31) >> 5;
     for (int x = wid; x < m3; x += nw) {
@@ -1048,8 +1057,9 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     if (tid == 0) s_m3 = cbase[kNumNb];
     __syncthreads();
   }
+  uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(J, sz, s_m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits),
-                    (int32_t*)(ws + lay.o_owner), t_old, t_new);
+                    (int32_t*)(ws + lay.o_owner), t_old, t_new, big);
 }
 
 // --------------------------------------------------------------------------
@@ -1089,6 +1099,11 @@ struct SoloLayout {
     total = align_up(e2 > e3 ? e2 : e3, 128);
   }
 };
+
+__host__ __device__ size_t ws_big_bits_offset(int size) {
+  const size_t c = MergeLayout(size).total * kClusterCtas, o = SoloLayout(size).total;
+  return align_up(c > o ? c : o, 256);
+}
 
 template <bool WIDE>
 __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __restrict__ jobs, int use_smem) {
@@ -1143,8 +1158,9 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
   int32_t* t_old = (int32_t*)(ws + lay.o_told);
   for (int p = tid; p < sz; p += nt) t_old[p] = J->tour[p];
   __syncthreads();
+  uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
-                     t_old, (int32_t*)(ws + lay.o_tnew));
+                     t_old, (int32_t*)(ws + lay.o_tnew), big);
 }
 
 // --------------------------------------------------------------------------
@@ -1320,8 +1336,9 @@ __global__ void __launch_bounds__(kMergeThreads) k_total_finish(const JobDev* __
   int32_t* t_old = (int32_t*)(ws + lay.o_told);
   for (int p = tid; p < sz; p += nt) t_old[p] = J->tour[p];
   __syncthreads();
+  uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
-                     t_old, (int32_t*)(ws + lay.o_tnew));
+                     t_old, (int32_t*)(ws + lay.o_tnew), big);
 }
 
 // --------------------------------------------------------------------------
@@ -1500,8 +1517,7 @@ cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* job
 
 size_t merge_smem_bytes(int size) { return MergeLayout(size).total; }
 size_t merge_ws_bytes(int size) {
-  const size_t c = MergeLayout(size).total * kClusterCtas, o = SoloLayout(size).total;
-  return c > o ? c : o;
+  return ws_big_bits_offset(size) + (MergeLayout(size).m3cap > kBitMax ? ws_big_bits_bytes() : 0);
 }
 size_t solo_smem_bytes(int size) { return SoloLayout(size).total; }
 int solo_smem_max_size() {

@@ -148,18 +148,36 @@ __device__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t*
   const int chunk = (sz + nt - 1) / nt;
   const int p0 = threadIdx.x * chunk;
   const int p1 = min(sz, p0 + chunk);
-  C sW = 0, sQ = 0, sC = 0;
-  for (int p = p0; p < p1; p++) {
+  auto gather = [&](int p) {
     const int32_t prev = p > 0 ? t[p - 1] : 0;
     const int32_t wp = p > 0 ? D[(size_t)prev * n + t[p]] : 0;
     w[p] = wp;
     w_s[p] = wp;
-    sW += (C)wp;
-    sQ += (C)p * (C)wp;
-    sC += (C)(sz - p) * (C)wp;
 #pragma unroll
     for (int k = 1; k <= 3; k++)
       A[(k - 1) * pad + p] = (p >= 1 && p + k <= sz - 1) ? D[(size_t)prev * n + t[p + k]] : 0;
+    return wp;
+  };
+  C sW = 0, sQ = 0, sC = 0;
+  if (chunk == 1) {  // one position per thread at most
+    if (p0 < p1) {
+      const C wp = (C)gather(p0);
+      sW = wp;
+      sQ = (C)p0 * wp;
+      sC = (C)(sz - p0) * wp;
+    }
+  } else {
+    // Gathers first, strided so that each thread's positions are independent
+    // (several in flight); then the per-thread contiguous chunks of the scan.
+#pragma unroll 4
+    for (int p = threadIdx.x; p < sz; p += nt) gather(p);
+    __syncthreads();
+    for (int p = p0; p < p1; p++) {
+      const C wp = (C)w_s[p];
+      sW += wp;
+      sQ += (C)p * wp;
+      sC += (C)(sz - p) * wp;
+    }
   }
   C totW, totQ, totC, eW, eQ;
   block_exclusive_scan3<C>(sW, sQ, sC, smW, smQ, smC, eW, eQ, totW, totQ, totC);

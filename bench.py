@@ -112,30 +112,47 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    PERIOD_MS = 50
+
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
         self.t = None
+        self.t_begin = None
 
     def start(self):
+        """Starts nvidia-smi and waits (up to 5 s) for its first sample, so
+        that the sampling is running when the timed region begins."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
             return
         self.t = threading.Thread(target=self._read, daemon=True)
         self.t.start()
+        t_end = time.perf_counter() + 5.0
+        while not self.lines and self.proc.poll() is None and time.perf_counter() < t_end:
+            time.sleep(0.01)
+
+    def begin(self):
+        """Marks the start of the timed region."""
+        self.t_begin = time.perf_counter()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def stop(self) -> dict:
+        """Ends sampling; keeps the samples taken during the timed region (from
+        begin() to now, plus one sampling period), or the first one after it
+        starts when the region was shorter than a period."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        t_stop = time.perf_counter()
+        time.sleep(self.PERIOD_MS / 1000.0)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -143,9 +160,13 @@ class ClockSampler:
             self.proc.kill()
         if self.t:
             self.t.join(timeout=2)
+        t0 = self.t_begin if self.t_begin is not None else 0.0
+        kept = [ln for ts, ln in self.lines if t0 <= ts <= t_stop + self.PERIOD_MS / 1000.0]
+        if not kept:
+            kept = [ln for ts, ln in self.lines if ts >= t0][:1]
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in kept:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -348,12 +369,13 @@ def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
     # DVND steps: device time, start tours already resident in HBM, L2 flushed.
     step_ms, step_evals, step_sweeps, costs = [], [], [], []
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
     for k in range(nsteps):
         if k == args.warmup:
-            sampler.start()
             if world > 1:
                 torch.distributed.barrier()
             torch.cuda.synchronize()
+            sampler.begin()
         e0, e1 = _events(2)
         with torch.cuda.stream(stream):
             flush.zero_()

@@ -270,31 +270,76 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   // used its sweep limit is skipped before its distance gathers.
   const bool done = stats[kStatConverged] || stats[kStatSweeps] >= stats[kStatLimit];
 
-  for (int q = tid; q < SR; q += TL) {
-    const int p = r0 - 1 + q;
-    sRowT[q] = p <= sz - 1 ? t[p] : 0;
-  }
-  for (int q = tid; q < NT; q += TL) {
-    const int p = r0 + L0 - 2 + q;
-    sColT[q] = p <= sz - 1 ? t[p] : 0;
-  }
-  for (int q = tid; q < NR; q += TL) {
-    const int p = r0 + q;
-    const bool ok = p < pad;
-    sRw[q] = ok ? w[p] : 0;
-    sRW[q] = ok ? W[p] : C(0);
-    sRQ[q] = ok ? Q[p] : C(0);
+  {
+    // Tour positions and per-position arrays of the tile's rows and columns:
+    // every load is issued before any is stored, so the tile pays one L2
+    // round trip here instead of one per array.
+    constexpr int kSR = (SR + TL - 1) / TL, kNT = (NT + TL - 1) / TL;
+    constexpr int kNR = (NR + TL - 1) / TL, kNC = (NC + TL - 1) / TL;
+    int32_t vRT[kSR], vCT[kNT], vRw[kNR], vRA[3][kNR], vCw[kNC], vCA[3][kNC];
+    C vRW[kNR], vRQ[kNR], vCW[kNC], vCQ[kNC];
 #pragma unroll
-    for (int k = 0; k < 3; k++) sRA[k][q] = ok ? Ag[k * pad + p] : 0;
-  }
-  for (int q = tid; q < NC; q += TL) {
-    const int p = r0 + L0 - 1 + q;
-    const bool ok = p < pad;
-    sCw[q] = ok ? w[p] : 0;
-    sCW[q] = ok ? W[p] : C(0);
-    sCQ[q] = ok ? Q[p] : C(0);
+    for (int u = 0; u < kSR; u++) {
+      const int q = tid + u * TL, p = r0 - 1 + q;
+      vRT[u] = (q < SR && p <= sz - 1) ? t[p] : 0;
+    }
 #pragma unroll
-    for (int k = 0; k < 3; k++) sCA[k][q] = ok ? Ag[k * pad + p] : 0;
+    for (int u = 0; u < kNT; u++) {
+      const int q = tid + u * TL, p = r0 + L0 - 2 + q;
+      vCT[u] = (q < NT && p <= sz - 1) ? t[p] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kNR; u++) {
+      const int q = tid + u * TL, p = r0 + q;
+      const bool ok = q < NR && p < pad;
+      vRw[u] = ok ? w[p] : 0;
+      vRW[u] = ok ? W[p] : C(0);
+      vRQ[u] = ok ? Q[p] : C(0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) vRA[k][u] = ok ? Ag[k * pad + p] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kNC; u++) {
+      const int q = tid + u * TL, p = r0 + L0 - 1 + q;
+      const bool ok = q < NC && p < pad;
+      vCw[u] = ok ? w[p] : 0;
+      vCW[u] = ok ? W[p] : C(0);
+      vCQ[u] = ok ? Q[p] : C(0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) vCA[k][u] = ok ? Ag[k * pad + p] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kSR; u++) {
+      const int q = tid + u * TL;
+      if (q < SR) sRowT[q] = vRT[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kNT; u++) {
+      const int q = tid + u * TL;
+      if (q < NT) sColT[q] = vCT[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kNR; u++) {
+      const int q = tid + u * TL;
+      if (q < NR) {
+        sRw[q] = vRw[u];
+        sRW[q] = vRW[u];
+        sRQ[q] = vRQ[u];
+#pragma unroll
+        for (int k = 0; k < 3; k++) sRA[k][q] = vRA[k][u];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kNC; u++) {
+      const int q = tid + u * TL;
+      if (q < NC) {
+        sCw[q] = vCw[u];
+        sCW[q] = vCW[u];
+        sCQ[q] = vCQ[u];
+#pragma unroll
+        for (int k = 0; k < 3; k++) sCA[k][q] = vCA[k][u];
+      }
+    }
   }
   __syncthreads();
   if (done) return;

@@ -134,7 +134,7 @@ __device__ void block_exclusive_scan3(T a, T b, T c, T* sa, T* sb, T* sc, T& ea,
 // (source/mlsolution.cpp:216-228 and :454-458 for T = W).
 // --------------------------------------------------------------------------
 template <bool WIDE>
-__device__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t* w_s) {
+__device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t* w_s) {
   using C = typename Arith<WIDE>::C;
   __shared__ C smW[32], smQ[32], smC[32];
   const int sz = J->size, n = J->n, pad = sz + 8;
@@ -679,7 +679,7 @@ __device__ __forceinline__ int group_sync_or(int pred, int id, int nthreads) {
 //              are small: the first alive candidate is kept and its conflicts
 //              removed, repeatedly.
 // On return st[x] == kIn marks the kept candidates.
-__device__ void stage2_group(int nb, int sz, int m, int gtid, int gnt, int bar, Rec* rec, uint64_t* tables,
+__device__ __forceinline__ void stage2_group(int nb, int sz, int m, int gtid, int gnt, int bar, Rec* rec, uint64_t* tables,
                              uint64_t* gmin) {
   if (nb == 0) {
     uint64_t* minK = tables;
@@ -774,7 +774,7 @@ __device__ void stage2_group(int nb, int sz, int m, int gtid, int gnt, int bar, 
 // candidate with a negative delta becomes a kUndec record keyed
 // (delta, block), with its move in ij (i | j << 16) and its conflict interval
 // (2-opt, Or-opt) or endpoints (swap) in ab; the other blocks get kNone.
-__device__ void stage2_records(const JobDev* J, int nb, int sz, Rec* rec, uint32_t* ij) {
+__device__ __forceinline__ void stage2_records(const JobDev* J, int nb, int sz, Rec* rec, uint32_t* ij) {
   const int m = nb_blocks(nb, sz), off = nb_offset(nb, sz);
   const int tid = threadIdx.x, nt = blockDim.x;
   const uint64_t* keys = J->keys + off;
@@ -827,7 +827,7 @@ __device__ __forceinline__ int id_of(uint64_t key3) { return (int)((key3 >> kCtx
 // workspace (bits: min(m3, kBitMax)^2 bits); bits_big (may be null) holds
 // kBitMaxWs^2 bits for lists longer than kBitMax (global merge workspaces).
 template <bool WIDE>
-__device__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* key3, const uint64_t* shp3,
+__device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* key3, const uint64_t* shp3,
                              const uint32_t* ij3, volatile uint8_t* st3, uint32_t* bits, int32_t* owner,
                              int32_t* t_old, int32_t* t_new, uint32_t* bits_big = nullptr) {
   __shared__ uint32_t s_in[kBitMaxWs / 32], s_und[kBitMaxWs / 32];
@@ -978,9 +978,10 @@ __device__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* ke
 // canMerge, mlkernel.cu:649-864 with a stable order), the parallel apply of
 // the selected moves (footprints are disjoint for every pair canMerge
 // accepts), the ADS prefix rebuild and the candidate-key reset.
-template <bool WIDE>
+template <bool WIDE, bool SMEM>
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThreads)
-    k_merge(const JobDev* __restrict__ jobs, int use_smem) {
+    k_merge(const JobDev* __restrict__ jobs) {
+  constexpr bool use_smem = SMEM;
   extern __shared__ __align__(16) uint8_t dsm[];
   __shared__ uint64_t s_gmin[64];  // two step buffers of one entry per warp
   __shared__ int s_m3, s_cnt, s_err;
@@ -1052,6 +1053,13 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     if (tid == 0) st_release_cluster(&lead_flags[nb], count + 1);  // publishes the writes above
     return;
   }
+  // ---- leader: its own list through its own workspace pointer (the same
+  // bytes as through the cluster window; in shared memory the compiler then
+  // addresses them as shared memory) ----
+  key3 = (uint64_t*)(ws + lay.o_key3);
+  shp3 = (uint64_t*)(ws + lay.o_shp3);
+  ij3 = (uint32_t*)(ws + lay.o_ij3);
+  st3 = (volatile uint8_t*)(ws + lay.o_st3);
   // ---- leader: wait for the five neighbourhoods (bounded), then compact ----
   if (tid == 0) {
     s_err = 0;
@@ -1168,8 +1176,9 @@ __host__ __device__ size_t ws_big_bits_offset(int size) {
   return align_up(c > o ? c : o, 256);
 }
 
-template <bool WIDE>
-__global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __restrict__ jobs, int use_smem) {
+template <bool WIDE, bool SMEM>
+__global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __restrict__ jobs) {
+  constexpr bool use_smem = SMEM;
   extern __shared__ __align__(16) uint8_t dsm[];
   __shared__ uint64_t s_gmin[64];
   __shared__ int s_m3;
@@ -1362,8 +1371,9 @@ __global__ void __launch_bounds__(1024) k_oropt_pass(const JobDev* __restrict__ 
 // the cross-neighbourhood greedy, the apply and the ADS rebuild as after
 // k_merge_solo.  One 1024-thread CTA per job (the k_merge_solo workspace).
 // --------------------------------------------------------------------------
-template <bool WIDE>
-__global__ void __launch_bounds__(kMergeThreads) k_total_finish(const JobDev* __restrict__ jobs, int use_smem) {
+template <bool WIDE, bool SMEM>
+__global__ void __launch_bounds__(kMergeThreads) k_total_finish(const JobDev* __restrict__ jobs) {
+  constexpr bool use_smem = SMEM;
   extern __shared__ __align__(16) uint8_t dsm[];
   const JobDev* J = jobs + blockIdx.x;
   {
@@ -1639,8 +1649,13 @@ cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool u
                                 cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
   const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
-  if (wide) k_total_finish<true><<<njobs, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
-  else k_total_finish<false><<<njobs, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  if (wide) {
+    if (use_smem) k_total_finish<true, true><<<njobs, kMergeThreads, smem, s>>>(jobs);
+    else k_total_finish<true, false><<<njobs, kMergeThreads, smem, s>>>(jobs);
+  } else {
+    if (use_smem) k_total_finish<false, true><<<njobs, kMergeThreads, smem, s>>>(jobs);
+    else k_total_finish<false, false><<<njobs, kMergeThreads, smem, s>>>(jobs);
+  }
   return cudaGetLastError();
 }
 
@@ -1683,18 +1698,18 @@ cudaError_t configure_merge(size_t bytes) {
   // process: never lower it below the largest shared-memory merge layout, or
   // a set configured earlier with larger jobs would fail its next launch.
   bytes = bytes > MergeLayout(merge_smem_max_size()).total ? bytes : MergeLayout(merge_smem_max_size()).total;
-  cudaError_t e = cudaFuncSetAttribute(k_merge<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = cudaFuncSetAttribute(k_merge<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_merge<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  e = cudaFuncSetAttribute(k_merge<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
   const int solo = (int)SoloLayout(solo_smem_max_size()).total;
-  e = cudaFuncSetAttribute(k_merge_solo<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  e = cudaFuncSetAttribute(k_merge_solo<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_merge_solo<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  e = cudaFuncSetAttribute(k_merge_solo<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_total_finish<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  e = cudaFuncSetAttribute(k_total_finish<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_total_finish<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
+  e = cudaFuncSetAttribute(k_total_finish<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solo);
   if (e != cudaSuccess) return e;
   return configure_total();
 }
@@ -1703,8 +1718,14 @@ cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem
                          cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
   const size_t smem = use_smem ? MergeLayout(max_size).total : 0;
-  if (wide) k_merge<true><<<njobs * kClusterCtas, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
-  else k_merge<false><<<njobs * kClusterCtas, kMergeThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  const unsigned g = (unsigned)(njobs * kClusterCtas);
+  if (wide) {
+    if (use_smem) k_merge<true, true><<<g, kMergeThreads, smem, s>>>(jobs);
+    else k_merge<true, false><<<g, kMergeThreads, smem, s>>>(jobs);
+  } else {
+    if (use_smem) k_merge<false, true><<<g, kMergeThreads, smem, s>>>(jobs);
+    else k_merge<false, false><<<g, kMergeThreads, smem, s>>>(jobs);
+  }
   return cudaGetLastError();
 }
 
@@ -1712,8 +1733,13 @@ cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use
                               cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
   const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
-  if (wide) k_merge_solo<true><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
-  else k_merge_solo<false><<<njobs, kSoloThreads, smem, s>>>(jobs, use_smem ? 1 : 0);
+  if (wide) {
+    if (use_smem) k_merge_solo<true, true><<<njobs, kSoloThreads, smem, s>>>(jobs);
+    else k_merge_solo<true, false><<<njobs, kSoloThreads, smem, s>>>(jobs);
+  } else {
+    if (use_smem) k_merge_solo<false, true><<<njobs, kSoloThreads, smem, s>>>(jobs);
+    else k_merge_solo<false, false><<<njobs, kSoloThreads, smem, s>>>(jobs);
+  }
   return cudaGetLastError();
 }
 

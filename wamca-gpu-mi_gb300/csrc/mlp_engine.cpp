@@ -933,7 +933,7 @@ int JobSet::read_stats(std::vector<std::array<int64_t, kStatWords>>* out) {
   int64_t err = 0;
   for (auto& a : *out) err |= a[kStatError];
   if (err) {
-    static const char* what[] = {"", "", "merge stage-2 hand-off timed out", "kept-move region overflow",
+    static const char* what[] = {"", "", "merge stage-2 hand-off timed out (no longer produced)", "kept-move region overflow",
                                  "TOTAL list overflow", "TOTAL selection invariant broken"};
     set_error(std::string("device reported an internal error (code ") + std::to_string(err) + ": " +
               (err >= 2 && err <= 5 ? what[err] : "unknown") + ")");

@@ -634,7 +634,7 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
   return ((uint64_t)hi << 32) | lo;
 }
 
-// Split cluster barrier and cluster-scope release/acquire accesses.
+// Split cluster barrier.
 __device__ __forceinline__ void cluster_arrive_release() {
   asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
 }
@@ -642,15 +642,6 @@ __device__ __forceinline__ void cluster_arrive_relaxed() {
   asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
 }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
-__device__ __forceinline__ void st_release_cluster(int* p, int v) {
-  asm volatile("st.release.cluster.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ int ld_acquire_cluster(const int* p) {
-  int v;
-  asm volatile("ld.acquire.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void fence_acquire_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
 
 // Named barriers (ids 1..5) synchronise one warp group without the others.
 __device__ __forceinline__ void group_sync(int id, int nthreads) {
@@ -973,8 +964,13 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
 
 // One cluster of six CTAs per job.  CTAs 0..4 run stage 2 of neighbourhood
 // 0..4 with the whole CTA and hand their kept moves straight to CTA 5 (the
-// leader) through distributed shared memory; the leader, which has fetched the
-// current tour meanwhile, runs stage 3 (cross-neighbourhood greedy with
+// leader) through distributed shared memory.  Two phases of the hardware
+// cluster barrier order the hand-off: every CTA arrives at phase 1 when it
+// starts (a stage-2 CTA waits for it before its first remote write, so the
+// leader is running); a stage-2 CTA arrives at phase 2 with release semantics
+// once its moves and count are written, and the leader's acquire wait of
+// phase 2 sees all five lists.  Every CTA arrives and waits at both phases.
+// The leader, which has fetched the current tour meanwhile, runs stage 3 (cross-neighbourhood greedy with
 // canMerge, mlkernel.cu:649-864 with a stable order), the parallel apply of
 // the selected moves (footprints are disjoint for every pair canMerge
 // accepts), the ADS prefix rebuild and the candidate-key reset.
@@ -984,8 +980,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   constexpr bool use_smem = SMEM;
   extern __shared__ __align__(16) uint8_t dsm[];
   __shared__ uint64_t s_gmin[64];  // two step buffers of one entry per warp
-  __shared__ int s_m3, s_cnt, s_err;
-  __shared__ int s_flag[kNumNb];  // leader: count + 1 published by each stage-2 CTA
+  __shared__ int s_m3, s_cnt;
+  __shared__ int s_flag[kNumNb];  // leader: the kept-move count of each stage-2 CTA
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const JobDev* J = jobs + blockIdx.x / kClusterCtas;
@@ -1009,12 +1005,13 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   int32_t* t_old = (int32_t*)(ws + lay.o_told);
   int32_t* t_new = (int32_t*)(ws + lay.o_tnew);
   if (leader) {
-    if (tid < kNumNb) s_flag[tid] = 0;
-    __syncthreads();
-    cluster_arrive_release();  // the flags are initialised
+    cluster_arrive_relaxed();  // phase 1: this CTA runs
     for (int p = tid; p < sz; p += nt) t_old[p] = tour[p];  // completes while stage 2 runs
+    cluster_wait();            // phase 1
+    cluster_arrive_relaxed();  // phase 2: the leader has nothing to publish
+    cluster_wait();            // phase 2 (acquire): the five kept lists and counts
   } else {
-    cluster_arrive_relaxed();
+    cluster_arrive_relaxed();  // phase 1: this CTA runs
     const int nb = rank;
     int count = 0;
     if ((mask >> nb) & 1) {
@@ -1030,7 +1027,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
       int nmine = 0;
       for (int x = tid; x < m; x += nt) nmine += rec[x].st == kIn;
       int slot = nmine ? atomicAdd(&s_cnt, nmine) : 0;
-      cluster_wait();  // the leader's flags are initialised (arrivals overlap stage 2)
+      cluster_wait();  // phase 1: the leader runs (the arrivals overlapped stage 2)
       const int base = region_off(nb, sz), cap = region_cap(nb, sz);
       for (int x = tid; x < m; x += nt) {
         if (rec[x].st != kIn) continue;
@@ -1043,14 +1040,16 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
         }
         slot++;
       }
-      fence_acquire_cluster();  // this thread's remote writes, before the flag below
       __syncthreads();
       count = min(s_cnt, cap);
       if (tid == 0 && s_cnt > cap) J->stats[kStatError] = 3;
     } else {
-      cluster_wait();
+      cluster_wait();  // phase 1
     }
-    if (tid == 0) st_release_cluster(&lead_flags[nb], count + 1);  // publishes the writes above
+    if (tid == 0) lead_flags[nb] = count;
+    __syncwarp();
+    cluster_arrive_release();  // phase 2: publishes this thread's remote writes
+    cluster_wait();            // phase 2
     return;
   }
   // ---- leader: its own list through its own workspace pointer (the same
@@ -1060,30 +1059,12 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   shp3 = (uint64_t*)(ws + lay.o_shp3);
   ij3 = (uint32_t*)(ws + lay.o_ij3);
   st3 = (volatile uint8_t*)(ws + lay.o_st3);
-  // ---- leader: wait for the five neighbourhoods (bounded), then compact ----
-  if (tid == 0) {
-    s_err = 0;
-    long long spins = 0;
-    for (;;) {
-      int ready = 0;
-      for (int nb = 0; nb < kNumNb; nb++) ready += ld_acquire_cluster(&s_flag[nb]) != 0;
-      if (ready == kNumNb) break;
-      if (++spins > (1ll << 26)) {
-        J->stats[kStatError] = 2;
-        s_err = 1;
-        break;
-      }
-      __nanosleep(64);
-    }
-  }
-  __syncthreads();
-  fence_acquire_cluster();
-  if (s_err) return;
+  // ---- leader: compact the five regions ----
   {
     int cbase[kNumNb + 1];
     cbase[0] = 0;
 #pragma unroll
-    for (int nb = 0; nb < kNumNb; nb++) cbase[nb + 1] = cbase[nb] + (s_flag[nb] - 1);
+    for (int nb = 0; nb < kNumNb; nb++) cbase[nb + 1] = cbase[nb] + s_flag[nb];
     // Region offsets (constant divisors once the loop is unrolled).
     int roff[kNumNb];
     roff[0] = 0;

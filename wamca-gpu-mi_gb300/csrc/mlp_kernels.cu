@@ -578,6 +578,7 @@ struct __align__(16) Rec {
 };
 constexpr int kBitMax = 512;         // stage-3 conflict bit-matrix capacity (moves)
 constexpr int kBitMaxWs = 4096;      // the same in a global merge workspace (large tours: 2 MB)
+constexpr int kWarpRoundWords = 4;   // stage-3 lists up to 128 moves: one-warp rounds
 constexpr int kMergeThreads = 1024;
 constexpr int kClusterCtas = 6;  // five stage-2 CTAs and the stage-3 leader
 
@@ -843,6 +844,54 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
         if (lane == 0) bits[x * W3 + w] = word;
       }
     }
+    if (W3 <= kWarpRoundWords) {
+      // Up to 32 * kWarpRoundWords moves: one warp runs the rounds with the
+      // rows in registers (lane l holds moves l, l + 32, ...) and the kept /
+      // undecided masks as ballots, with no CTA barrier per round.
+      __syncthreads();
+      if (wid == 0) {
+        uint32_t row[kWarpRoundWords][kWarpRoundWords];
+        uint8_t st[kWarpRoundWords];
+        uint32_t in[kWarpRoundWords], und[kWarpRoundWords];
+#pragma unroll
+        for (int q = 0; q < kWarpRoundWords; q++) {
+          const int x = 32 * q + lane;
+          st[q] = (q < W3 && x < m3) ? kUndec : kNone;
+#pragma unroll
+          for (int w = 0; w < kWarpRoundWords; w++) row[q][w] = (st[q] == kUndec && w < W3) ? bits[x * W3 + w] : 0u;
+          in[q] = 0u;
+          und[q] = __ballot_sync(kFull, st[q] == kUndec);
+        }
+        for (int round = 0; round <= m3; round++) {
+#pragma unroll
+          for (int q = 0; q < kWarpRoundWords; q++) {
+            if (st[q] != kUndec) continue;
+            uint32_t hin = 0, hund = 0;
+#pragma unroll
+            for (int w = 0; w < kWarpRoundWords; w++) {
+              hin |= row[q][w] & in[w];
+              hund |= row[q][w] & und[w];
+            }
+            if (hin) st[q] = kOut;
+            else if (!hund) st[q] = kIn;
+          }
+          uint32_t left = 0;
+#pragma unroll
+          for (int q = 0; q < kWarpRoundWords; q++) {
+            in[q] = __ballot_sync(kFull, st[q] == kIn);
+            und[q] = __ballot_sync(kFull, st[q] == kUndec);
+            left |= und[q];
+          }
+          if (!left) break;
+        }
+#pragma unroll
+        for (int q = 0; q < kWarpRoundWords; q++) {
+          const int x = 32 * q + lane;
+          if (q < W3 && x < m3) st3[x] = st[q];
+        }
+      }
+      __syncthreads();
+    } else {
     for (int w = tid; w < W3; w += nt) {
       s_in[w] = 0;
       const int rem = m3 - 32 * w;
@@ -874,6 +923,7 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
         }
       }
       if (!__syncthreads_or(any)) break;
+    }
     }
   } else {
     // long lists: one warp per undecided move scans the earlier ones

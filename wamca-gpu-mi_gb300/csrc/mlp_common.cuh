@@ -224,34 +224,36 @@ MLP_HD void conflict_interval(int id, int i, int j, int& a, int& b) {
   }
 }
 
-// Branch-free form of !canMerge for the cross-neighbourhood merge.  A move's
-// shape is its type (0 swap, 1 2-opt, 2 Or-opt) and two closed core intervals:
-// swap {i}, {j}; 2-opt [i, j] twice; Or-opt-k [min, max+k] twice.  Two moves
-// conflict iff a core interval of the lower type meets a core interval of the
-// higher type widened by one position on the left (unless both are Or-opt)
-// and on the right (unless the higher type is Or-opt).  Exhaustively equal to
-// !canMerge (mlkernel.cu:649-729) over every move pair of small tours.
+// Branch-free form of !canMerge for the cross-neighbourhood merge.  canMerge
+// (mlkernel.cu:649-729) rejects a pair when a core interval of the move of
+// lower type (0 swap: {i}, {j}; 1 2-opt: [i, j]; 2 Or-opt-k: [min, max+k])
+// meets a core interval of the other move widened by one position on the left
+// unless the lower type is Or-opt, and on the right unless the higher type is
+// Or-opt.  With e(t) = 0 for Or-opt and 1 otherwise that is
+//   la <= hb + e(t_hi)  and  ha - e(t_lo) <= lb,
+// i.e. [la, lb + e(t_lo)] and [ha, hb + e(t_hi)] intersect: widening every
+// move's own intervals by e of its own type on the right makes the test
+// symmetric and free of the types.  A shape packs the two right-widened
+// intervals as four 16-bit fields (a1, b1, a2, b2); a pair conflicts iff one
+// of its four interval pairs intersects.  Exhaustively equal to !canMerge
+// over every move pair of small tours (tests/shape_conflict_check.cpp).
 MLP_HD uint64_t move_shape(int id, int i, int j) {
-  uint64_t t, a1, b1, a2, b2;
+  uint32_t a1, b1, a2, b2;
   if (id == 0) {
-    t = 0; a1 = b1 = (uint64_t)i; a2 = b2 = (uint64_t)j;
+    a1 = (uint32_t)i; b1 = (uint32_t)i + 1u; a2 = (uint32_t)j; b2 = (uint32_t)j + 1u;
   } else if (id == 1) {
-    t = 1; a1 = a2 = (uint64_t)i; b1 = b2 = (uint64_t)j;
+    a1 = a2 = (uint32_t)i; b1 = b2 = (uint32_t)j + 1u;
   } else {
-    t = 2; a1 = a2 = (uint64_t)imin_(i, j); b1 = b2 = (uint64_t)(imax_(i, j) + id - 1);
+    a1 = a2 = (uint32_t)imin_(i, j); b1 = b2 = (uint32_t)(imax_(i, j) + id - 1);
   }
-  return (t << 60) | (a1 << 45) | (b1 << 30) | (a2 << 15) | b2;
+  return (uint64_t)(a1 | (b1 << 16)) | ((uint64_t)(a2 | (b2 << 16)) << 32);
 }
 MLP_HD bool shapes_conflict(uint64_t s1, uint64_t s2) {
-  const int t1 = (int)(s1 >> 60), t2 = (int)(s2 >> 60);
-  const uint64_t lo = t1 <= t2 ? s1 : s2, hi = t1 <= t2 ? s2 : s1;
-  const int el = imin_(t1, t2) == 2 ? 0 : 1, er = imax_(t1, t2) == 2 ? 0 : 1;
-  const int la1 = (int)((lo >> 45) & 0x7fff), lb1 = (int)((lo >> 30) & 0x7fff);
-  const int la2 = (int)((lo >> 15) & 0x7fff), lb2 = (int)(lo & 0x7fff);
-  const int ha1 = (int)((hi >> 45) & 0x7fff) - el, hb1 = (int)((hi >> 30) & 0x7fff) + er;
-  const int ha2 = (int)((hi >> 15) & 0x7fff) - el, hb2 = (int)(hi & 0x7fff) + er;
-  return (la1 <= hb1 && ha1 <= lb1) | (la1 <= hb2 && ha2 <= lb1) | (la2 <= hb1 && ha1 <= lb2) |
-         (la2 <= hb2 && ha2 <= lb2);
+  const uint32_t p1 = (uint32_t)s1, p2 = (uint32_t)(s1 >> 32), q1 = (uint32_t)s2, q2 = (uint32_t)(s2 >> 32);
+  const uint32_t pa1 = p1 & 0xffffu, pb1 = p1 >> 16, pa2 = p2 & 0xffffu, pb2 = p2 >> 16;
+  const uint32_t qa1 = q1 & 0xffffu, qb1 = q1 >> 16, qa2 = q2 & 0xffffu, qb2 = q2 >> 16;
+  return (pa1 <= qb1 && qa1 <= pb1) | (pa1 <= qb2 && qa2 <= pb1) | (pa2 <= qb1 && qa1 <= pb2) |
+         (pa2 <= qb2 && qa2 <= pb2);
 }
 
 // ---------------- device job descriptor ----------------

@@ -131,10 +131,13 @@ __device__ void block_exclusive_scan3(T a, T b, T c, T* sa, T* sb, T* sc, T& ea,
 // --------------------------------------------------------------------------
 // ADS prefix rebuild: w[p] = D[t[p-1]][t[p]], W = prefix(w), Q = prefix(p w),
 // A[k-1][p] = D[t[p-1]][t[p+k]], cost = sum (size - p) w[p]
-// (source/mlsolution.cpp:216-228 and :454-458 for T = W).
+// (source/mlsolution.cpp:216-228 and :454-458 for T = W).  With t_prev, the
+// tour that J->w and J->A currently describe, a position whose window
+// t[p-1 .. p+3] is unchanged keeps its w and A (no distance gathers).
 // --------------------------------------------------------------------------
 template <bool WIDE>
-__device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t* w_s) {
+__device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t* w_s,
+                                            const int32_t* t_prev = nullptr) {
   using C = typename Arith<WIDE>::C;
   __shared__ C smW[32], smQ[32], smC[32];
   const int sz = J->size, n = J->n, pad = sz + 8;
@@ -149,6 +152,19 @@ __device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_ov
   const int p0 = threadIdx.x * chunk;
   const int p1 = min(sz, p0 + chunk);
   auto gather = [&](int p) {
+    if (t_prev != nullptr) {
+      bool same = true;
+#pragma unroll
+      for (int d = -1; d <= 3; d++) {
+        const int q = p + d;
+        if (q >= 0 && q < sz) same &= t[q] == t_prev[q];
+      }
+      if (same) {
+        const int32_t wp = w[p];
+        w_s[p] = wp;
+        return wp;
+      }
+    }
     const int32_t prev = p > 0 ? t[p - 1] : 0;
     const int32_t wp = p > 0 ? D[(size_t)prev * n + t[p]] : 0;
     w[p] = wp;
@@ -1008,7 +1024,7 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
     else atomicExch(&stt[kStatConverged], 1ull);
   }
   __syncthreads();
-  cta_prepare<WIDE>(J, t_new, t_old);  // t_old is free again: w staging
+  cta_prepare<WIDE>(J, t_new, owner, t_old);  // the owner map is dead: w staging
   cta_reset_keys(J);
 }
 

@@ -133,11 +133,12 @@ __device__ void block_exclusive_scan3(T a, T b, T c, T* sa, T* sb, T* sc, T& ea,
 // A[k-1][p] = D[t[p-1]][t[p+k]], cost = sum (size - p) w[p]
 // (source/mlsolution.cpp:216-228 and :454-458 for T = W).  With t_prev, the
 // tour that J->w and J->A currently describe, a position whose window
-// t[p-1 .. p+3] is unchanged keeps its w and A (no distance gathers).
+// t[p-1 .. p+3] is unchanged keeps its w and A (no distance gathers); w_prev,
+// when given, is a copy of J->w to read those from.
 // --------------------------------------------------------------------------
 template <bool WIDE>
 __device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t* w_s,
-                                            const int32_t* t_prev = nullptr) {
+                                            const int32_t* t_prev = nullptr, const int32_t* w_prev = nullptr) {
   using C = typename Arith<WIDE>::C;
   __shared__ C smW[32], smQ[32], smC[32];
   const int sz = J->size, n = J->n, pad = sz + 8;
@@ -160,7 +161,7 @@ __device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_ov
         if (q >= 0 && q < sz) same &= t[q] == t_prev[q];
       }
       if (same) {
-        const int32_t wp = w[p];
+        const int32_t wp = w_prev != nullptr ? w_prev[p] : w[p];
         w_s[p] = wp;
         return wp;
       }
@@ -609,7 +610,7 @@ struct MergeLayout {
   // stage-2 CTA: records, moves, swap tables
   size_t o_ij2, o_tab, s2;
   // leader: stage-3 list, conflict bits, owner map, old and new tour
-  size_t o_key3, o_shp3, o_ij3, o_st3, o_bits, o_owner, o_told, o_tnew, s3;
+  size_t o_key3, o_shp3, o_ij3, o_st3, o_bits, o_owner, o_told, o_tnew, o_wold, s3;
   size_t total;
   __host__ __device__ explicit MergeLayout(int size) {
     tb = total_blocks(size);
@@ -630,7 +631,8 @@ struct MergeLayout {
     o_owner = o_bits + (size_t)kBitMax * (kBitMax / 32) * 4;
     o_told = o_owner + align_up((size_t)size * 4, 16);
     o_tnew = o_told + align_up((size_t)size * 4, 16);
-    s3 = o_tnew + align_up((size_t)size * 4, 16);
+    o_wold = o_tnew + align_up((size_t)size * 4, 16);
+    s3 = o_wold + align_up((size_t)size * 4, 16);
     total = align_up(s2 > s3 ? s2 : s3, 128);
   }
 };
@@ -833,11 +835,13 @@ __device__ __forceinline__ int id_of(uint64_t key3) { return (int)((key3 >> kCtx
 // key3 / shp3 / ij3 / st3[0, m3) of kept stage-2 moves (any order; every
 // st3 entry kUndec).  t_old holds the current tour; bits, owner and t_new are
 // workspace (bits: min(m3, kBitMax)^2 bits); bits_big (may be null) holds
-// kBitMaxWs^2 bits for lists longer than kBitMax (global merge workspaces).
+// kBitMaxWs^2 bits for lists longer than kBitMax (global merge workspaces);
+// w_old (may be null) is a copy of J->w for the prefix rebuild.
 template <bool WIDE>
 __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* key3, const uint64_t* shp3,
                              const uint32_t* ij3, volatile uint8_t* st3, uint32_t* bits, int32_t* owner,
-                             int32_t* t_old, int32_t* t_new, uint32_t* bits_big = nullptr) {
+                             int32_t* t_old, int32_t* t_new, uint32_t* bits_big = nullptr,
+                             const int32_t* w_old = nullptr) {
   __shared__ uint32_t s_in[kBitMaxWs / 32], s_und[kBitMaxWs / 32];
   __shared__ int s_ns;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -1024,7 +1028,7 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
     else atomicExch(&stt[kStatConverged], 1ull);
   }
   __syncthreads();
-  cta_prepare<WIDE>(J, t_new, owner, t_old);  // the owner map is dead: w staging
+  cta_prepare<WIDE>(J, t_new, owner, t_old, w_old);  // the owner map is dead: w staging
   cta_reset_keys(J);
 }
 
@@ -1048,6 +1052,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   __shared__ uint64_t s_gmin[64];  // two step buffers of one entry per warp
   __shared__ int s_m3, s_cnt;
   __shared__ int s_flag[kNumNb];  // leader: the kept-move count of each stage-2 CTA
+  __shared__ JobDev s_job;        // leader: its copy of the job descriptor
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const JobDev* J = jobs + blockIdx.x / kClusterCtas;
@@ -1070,9 +1075,20 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   const bool leader = rank == kClusterCtas - 1;
   int32_t* t_old = (int32_t*)(ws + lay.o_told);
   int32_t* t_new = (int32_t*)(ws + lay.o_tnew);
+  // In shared memory the leader keeps a copy of w (a global workspace gains
+  // nothing from one: the prefix rebuild reads J->w).
+  int32_t* w_old = use_smem ? (int32_t*)(ws + lay.o_wold) : nullptr;
   if (leader) {
     cluster_arrive_relaxed();  // phase 1: this CTA runs
-    for (int p = tid; p < sz; p += nt) t_old[p] = tour[p];  // completes while stage 2 runs
+    // Copies that complete while stage 2 runs: the tour and, in shared memory,
+    // the job descriptor (its later field reads stay on chip) and w.
+    static_assert(sizeof(JobDev) % 8 == 0, "JobDev copy in 8-byte words");
+    if (use_smem && tid < (int)(sizeof(JobDev) / 8)) ((uint64_t*)&s_job)[tid] = ((const uint64_t*)J)[tid];
+    const int32_t* w_cur = J->w;
+    for (int p = tid; p < sz; p += nt) {
+      t_old[p] = tour[p];
+      if (use_smem) w_old[p] = w_cur[p];
+    }
     cluster_wait();            // phase 1
     cluster_arrive_relaxed();  // phase 2: the leader has nothing to publish
     cluster_wait();            // phase 2 (acquire): the five kept lists and counts
@@ -1176,8 +1192,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     __syncthreads();
   }
   uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
-  merge_finish<WIDE>(J, sz, s_m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits),
-                    (int32_t*)(ws + lay.o_owner), t_old, t_new, big);
+  merge_finish<WIDE>(use_smem ? &s_job : J, sz, s_m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits),
+                     (int32_t*)(ws + lay.o_owner), t_old, t_new, big, w_old);
 }
 
 // --------------------------------------------------------------------------

@@ -880,7 +880,7 @@ def run_ours(args, world, rank, local) -> None:
                                   "(profiles/dvnd_n1000_launches.md); the roofline above is the sweep's, the "
                                   "bandwidth kernel; the merge is latency-bound (critical path of the greedy "
                                   "rounds and barriers, 0.6 MB of traffic)",
-                          "k_merge": 0.630, "k_sweep": 0.355},
+                          "k_merge": 0.627, "k_sweep": 0.354},
     }
     line.update(extra)
     if not args.no_cpu:

@@ -202,18 +202,21 @@ def test_matrix_problem_and_errors(mlpgpu_mod):
     assert s.dvnd()["cost"] == oracle.dvnd(t, D)[1]["cost"]
 
 
-def test_large_sizes_use_global_merge_workspace(mlpgpu_mod):
-    """Sizes beyond the shared-memory merge run the merge from a global
-    workspace; alone and mixed with small jobs in one batch."""
-    n = 1900
+@pytest.mark.parametrize("n", [1900, 4200, 4500])
+def test_large_sizes_use_global_merge_workspace(mlpgpu_mod, n):
+    """The cluster merge's workspace around its shared-memory limit (tour
+    size 4419: n = 4418): n = 1900 well inside it; n = 4200 inside it without
+    the leader's copy of w (the copy would not fit); n = 4500 beyond it, from a
+    global workspace.  Alone and mixed with a small job in one batch."""
     x, y = oracle.uniform_instance(n, 51)
     D = oracle.dist(x, y, True)
     t = oracle.random_perm_tour(n, 51)
     p = mlpgpu_mod.Problem.from_coords(x, y, dist_round=True)
     s = mlpgpu_mod.Solver(p)
     s.set_tour(t)
-    st = s.dvnd(max_iters=6)
-    ot, ost = oracle.dvnd(t, D, max_iters=6, threads=8)
+    iters = 6 if n < 4000 else 3
+    st = s.dvnd(max_iters=iters)
+    ot, ost = oracle.dvnd(t, D, max_iters=iters, threads=8)
     assert np.array_equal(s.tour(), ot) and st["cost"] == ost["cost"]
     b = mlpgpu_mod.Batch()
     xs, ys = oracle.uniform_instance(80, 52)
@@ -222,8 +225,8 @@ def test_large_sizes_use_global_merge_workspace(mlpgpu_mod):
     ps = mlpgpu_mod.Problem.from_coords(xs, ys, dist_round=True)
     b.add(ps, ts)
     b.add(p, t)
-    b.run(max_iters=6)
-    assert np.array_equal(b.result(0)[0], oracle.dvnd(ts, Ds, max_iters=6)[0])
+    b.run(max_iters=iters)
+    assert np.array_equal(b.result(0)[0], oracle.dvnd(ts, Ds, max_iters=iters)[0])
     assert np.array_equal(b.result(1)[0], ot)
 
 

@@ -598,6 +598,9 @@ constexpr int kBitMaxWs = 4096;      // the same in a global merge workspace (la
 constexpr int kWarpRoundWords = 4;   // stage-3 lists up to 128 moves: one-warp rounds
 constexpr int kMergeThreads = 1024;
 constexpr int kClusterCtas = 6;  // five stage-2 CTAs and the stage-3 leader
+// Dynamic shared memory a merge workspace may use: the 227 KB opt-in limit
+// less room for the kernels' static shared memory.
+constexpr size_t kMergeSmemLimit = 227 * 1024 - 4096;
 
 // Workspace layout (bytes) of the merge CTA of a job of a given size.
 //   A: per-candidate key / move / state of the five neighbourhoods (stage 2);
@@ -611,6 +614,7 @@ struct MergeLayout {
   size_t o_ij2, o_tab, s2;
   // leader: stage-3 list, conflict bits, owner map, old and new tour
   size_t o_key3, o_shp3, o_ij3, o_st3, o_bits, o_owner, o_told, o_tnew, o_wold, s3;
+  bool has_wold;  // the leader's copy of w fits (it is left out where it would cost shared-memory mode)
   size_t total;
   __host__ __device__ explicit MergeLayout(int size) {
     tb = total_blocks(size);
@@ -632,7 +636,9 @@ struct MergeLayout {
     o_told = o_owner + align_up((size_t)size * 4, 16);
     o_tnew = o_told + align_up((size_t)size * 4, 16);
     o_wold = o_tnew + align_up((size_t)size * 4, 16);
-    s3 = o_wold + align_up((size_t)size * 4, 16);
+    const size_t with_w = o_wold + align_up((size_t)size * 4, 16);
+    has_wold = align_up(s2 > with_w ? s2 : with_w, 128) <= kMergeSmemLimit;
+    s3 = has_wold ? with_w : o_wold;
     total = align_up(s2 > s3 ? s2 : s3, 128);
   }
 };
@@ -1077,7 +1083,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   int32_t* t_new = (int32_t*)(ws + lay.o_tnew);
   // In shared memory the leader keeps a copy of w (a global workspace gains
   // nothing from one: the prefix rebuild reads J->w).
-  int32_t* w_old = use_smem ? (int32_t*)(ws + lay.o_wold) : nullptr;
+  int32_t* w_old = (use_smem && lay.has_wold) ? (int32_t*)(ws + lay.o_wold) : nullptr;
   if (leader) {
     cluster_arrive_relaxed();  // phase 1: this CTA runs
     // Copies that complete while stage 2 runs: the tour and, in shared memory,
@@ -1087,7 +1093,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     const int32_t* w_cur = J->w;
     for (int p = tid; p < sz; p += nt) {
       t_old[p] = tour[p];
-      if (use_smem) w_old[p] = w_cur[p];
+      if (w_old != nullptr) w_old[p] = w_cur[p];
     }
     cluster_wait();            // phase 1
     cluster_arrive_relaxed();  // phase 2: the leader has nothing to publish
@@ -1671,7 +1677,7 @@ int merge_smem_max_size() {
   static int cached = 0;
   if (cached == 0) {
     int sz = 8;
-    while (sz < kMaxSize && MergeLayout(sz + 1).total <= (size_t)(227 * 1024 - 4096)) sz++;
+    while (sz < kMaxSize && MergeLayout(sz + 1).total <= kMergeSmemLimit) sz++;
     cached = sz;
   }
   return cached;

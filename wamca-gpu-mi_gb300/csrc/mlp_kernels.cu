@@ -1057,7 +1057,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   extern __shared__ __align__(16) uint8_t dsm[];
   __shared__ uint64_t s_gmin[64];  // two step buffers of one entry per warp
   __shared__ int s_m3, s_cnt;
-  __shared__ int s_flag[kNumNb];  // leader: the kept-move count of each stage-2 CTA
+  __shared__ int s_kept[kNumNb];  // leader: the kept-move count of each stage-2 CTA
   __shared__ JobDev s_job;        // leader: its copy of the job descriptor
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -1076,7 +1076,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   uint64_t* shp3 = (uint64_t*)(lead + lay.o_shp3);
   uint32_t* ij3 = (uint32_t*)(lead + lay.o_ij3);
   volatile uint8_t* st3 = (volatile uint8_t*)(lead + lay.o_st3);
-  int* lead_flags = cluster.map_shared_rank(s_flag, kClusterCtas - 1);
+  int* lead_kept = cluster.map_shared_rank(s_kept, kClusterCtas - 1);
   int32_t* tour = J->tour;
   const bool leader = rank == kClusterCtas - 1;
   int32_t* t_old = (int32_t*)(ws + lay.o_told);
@@ -1134,7 +1134,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     } else {
       cluster_wait();  // phase 1
     }
-    if (tid == 0) lead_flags[nb] = count;
+    if (tid == 0) lead_kept[nb] = count;
     __syncwarp();
     cluster_arrive_release();  // phase 2: publishes this thread's remote writes
     cluster_wait();            // phase 2
@@ -1152,7 +1152,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     int cbase[kNumNb + 1];
     cbase[0] = 0;
 #pragma unroll
-    for (int nb = 0; nb < kNumNb; nb++) cbase[nb + 1] = cbase[nb] + s_flag[nb];
+    for (int nb = 0; nb < kNumNb; nb++) cbase[nb + 1] = cbase[nb] + s_kept[nb];
     // Region offsets (constant divisors once the loop is unrolled).
     int roff[kNumNb];
     roff[0] = 0;

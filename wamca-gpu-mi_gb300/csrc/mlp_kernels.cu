@@ -683,6 +683,55 @@ __device__ __forceinline__ int group_sync_or(int pred, int id, int nthreads) {
   return r;
 }
 
+// Lexicographically-first maximal independent set of c <= 32 * kWarpRoundWords
+// moves by one warp (every lane calls it): word w of row x of `bits` (W words
+// a row) marks with bit y the earlier moves 32 w + y that conflict with move x.
+// Lane l holds moves l, l + 32, ... with their rows in registers; the kept and
+// undecided masks are ballots, so a round needs no CTA barrier.  On return
+// st_out[x] is kIn or kOut for every x < c.
+__device__ __forceinline__ void warp_lfmis(int c, int W, const uint32_t* bits, volatile uint8_t* st_out) {
+  const int lane = threadIdx.x & 31;
+  uint32_t row[kWarpRoundWords][kWarpRoundWords];
+  uint8_t st[kWarpRoundWords];
+  uint32_t in[kWarpRoundWords], und[kWarpRoundWords];
+#pragma unroll
+  for (int q = 0; q < kWarpRoundWords; q++) {
+    const int x = 32 * q + lane;
+    st[q] = (q < W && x < c) ? kUndec : kNone;
+#pragma unroll
+    for (int w = 0; w < kWarpRoundWords; w++) row[q][w] = (st[q] == kUndec && w < W) ? bits[x * W + w] : 0u;
+    in[q] = 0u;
+    und[q] = __ballot_sync(kFull, st[q] == kUndec);
+  }
+  for (int round = 0; round <= c; round++) {
+#pragma unroll
+    for (int q = 0; q < kWarpRoundWords; q++) {
+      if (st[q] != kUndec) continue;
+      uint32_t hin = 0, hund = 0;
+#pragma unroll
+      for (int w = 0; w < kWarpRoundWords; w++) {
+        hin |= row[q][w] & in[w];
+        hund |= row[q][w] & und[w];
+      }
+      if (hin) st[q] = kOut;
+      else if (!hund) st[q] = kIn;
+    }
+    uint32_t left = 0;
+#pragma unroll
+    for (int q = 0; q < kWarpRoundWords; q++) {
+      in[q] = __ballot_sync(kFull, st[q] == kIn);
+      und[q] = __ballot_sync(kFull, st[q] == kUndec);
+      left |= und[q];
+    }
+    if (!left) break;
+  }
+#pragma unroll
+  for (int q = 0; q < kWarpRoundWords; q++) {
+    const int x = 32 * q + lane;
+    if (q < W && x < c) st_out[x] = st[q];
+  }
+}
+
 // Stage 2 of one neighbourhood, run by one warp group: greedy independent set
 // of its negative candidates in (delta, block) order with the same-
 // neighbourhood predicate of the reference's GPU merge (mlkernel.cu:51-170
@@ -875,47 +924,7 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
       // rows in registers (lane l holds moves l, l + 32, ...) and the kept /
       // undecided masks as ballots, with no CTA barrier per round.
       __syncthreads();
-      if (wid == 0) {
-        uint32_t row[kWarpRoundWords][kWarpRoundWords];
-        uint8_t st[kWarpRoundWords];
-        uint32_t in[kWarpRoundWords], und[kWarpRoundWords];
-#pragma unroll
-        for (int q = 0; q < kWarpRoundWords; q++) {
-          const int x = 32 * q + lane;
-          st[q] = (q < W3 && x < m3) ? kUndec : kNone;
-#pragma unroll
-          for (int w = 0; w < kWarpRoundWords; w++) row[q][w] = (st[q] == kUndec && w < W3) ? bits[x * W3 + w] : 0u;
-          in[q] = 0u;
-          und[q] = __ballot_sync(kFull, st[q] == kUndec);
-        }
-        for (int round = 0; round <= m3; round++) {
-#pragma unroll
-          for (int q = 0; q < kWarpRoundWords; q++) {
-            if (st[q] != kUndec) continue;
-            uint32_t hin = 0, hund = 0;
-#pragma unroll
-            for (int w = 0; w < kWarpRoundWords; w++) {
-              hin |= row[q][w] & in[w];
-              hund |= row[q][w] & und[w];
-            }
-            if (hin) st[q] = kOut;
-            else if (!hund) st[q] = kIn;
-          }
-          uint32_t left = 0;
-#pragma unroll
-          for (int q = 0; q < kWarpRoundWords; q++) {
-            in[q] = __ballot_sync(kFull, st[q] == kIn);
-            und[q] = __ballot_sync(kFull, st[q] == kUndec);
-            left |= und[q];
-          }
-          if (!left) break;
-        }
-#pragma unroll
-        for (int q = 0; q < kWarpRoundWords; q++) {
-          const int x = 32 * q + lane;
-          if (q < W3 && x < m3) st3[x] = st[q];
-        }
-      }
+      if (wid == 0) warp_lfmis(m3, W3, bits, st3);
       __syncthreads();
     } else {
     for (int w = tid; w < W3; w += nt) {

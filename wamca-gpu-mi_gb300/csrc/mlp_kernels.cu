@@ -839,10 +839,12 @@ __device__ __forceinline__ void stage2_group(int nb, int sz, int m, int gtid, in
 // candidate with a negative delta becomes a kUndec record keyed
 // (delta, block), with its move in ij (i | j << 16) and its conflict interval
 // (2-opt, Or-opt) or endpoints (swap) in ab; the other blocks get kNone.
+// Every key read is reset to kKeyNone for the next sweep (nothing else reads
+// the keys after this point of a merge).
 __device__ __forceinline__ void stage2_records(const JobDev* J, int nb, int sz, Rec* rec, uint32_t* ij) {
   const int m = nb_blocks(nb, sz), off = nb_offset(nb, sz);
   const int tid = threadIdx.x, nt = blockDim.x;
-  const uint64_t* keys = J->keys + off;
+  uint64_t* keys = J->keys + off;
   constexpr int U = 4;
   for (int x0 = 0; x0 < m; x0 += U * nt) {
     uint64_t kv[U];
@@ -850,6 +852,11 @@ __device__ __forceinline__ void stage2_records(const JobDev* J, int nb, int sz, 
     for (int u = 0; u < U; u++) {
       const int x = x0 + u * nt + tid;
       kv[u] = x < m ? keys[x] : kKeyNone;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int x = x0 + u * nt + tid;
+      if (x < m && kv[u] != kKeyNone) keys[x] = kKeyNone;
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
@@ -891,12 +898,13 @@ __device__ __forceinline__ int id_of(uint64_t key3) { return (int)((key3 >> kCtx
 // st3 entry kUndec).  t_old holds the current tour; bits, owner and t_new are
 // workspace (bits: min(m3, kBitMax)^2 bits); bits_big (may be null) holds
 // kBitMaxWs^2 bits for lists longer than kBitMax (global merge workspaces);
-// w_old (may be null) is a copy of J->w for the prefix rebuild.
+// w_old (may be null) is a copy of J->w for the prefix rebuild; without
+// reset_keys the candidate keys were reset as stage 2 read them.
 template <bool WIDE>
 __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* key3, const uint64_t* shp3,
                              const uint32_t* ij3, volatile uint8_t* st3, uint32_t* bits, int32_t* owner,
                              int32_t* t_old, int32_t* t_new, uint32_t* bits_big = nullptr,
-                             const int32_t* w_old = nullptr) {
+                             const int32_t* w_old = nullptr, bool reset_keys = true) {
   __shared__ uint32_t s_in[kBitMaxWs / 32], s_und[kBitMaxWs / 32];
   __shared__ int s_ns;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -1044,7 +1052,8 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
   }
   __syncthreads();
   cta_prepare<WIDE>(J, t_new, owner, t_old, w_old);  // the owner map is dead: w staging
-  cta_reset_keys(J);
+  if (reset_keys) cta_reset_keys(J);
+  else if (J->tcount != nullptr && tid < kNumNb) J->tcount[tid] = 0;
 }
 
 // One cluster of six CTAs per job.  CTAs 0..4 run stage 2 of neighbourhood
@@ -1208,7 +1217,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   }
   uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(use_smem ? &s_job : J, sz, s_m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits),
-                     (int32_t*)(ws + lay.o_owner), t_old, t_new, big, w_old);
+                     (int32_t*)(ws + lay.o_owner), t_old, t_new, big, w_old, false);
 }
 
 // --------------------------------------------------------------------------
@@ -1310,7 +1319,7 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
   __syncthreads();
   uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
-                     t_old, (int32_t*)(ws + lay.o_tnew), big);
+                     t_old, (int32_t*)(ws + lay.o_tnew), big, nullptr, false);
 }
 
 // --------------------------------------------------------------------------

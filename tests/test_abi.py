@@ -112,3 +112,26 @@ def test_tuning_table_set_get_load_and_validation(tmp_path):
         assert mlpgpu.tuning_table() == []
     finally:
         mlpgpu.set_tuning_table(saved)
+
+
+def test_argument_validation_needs_no_gpu(built_lib):
+    """Malformed arguments are rejected with status codes and a message before
+    any device call (MLP_ERR_ARG = 1, MLP_ERR_RANGE = 3)."""
+    import ctypes as C
+
+    import numpy as np
+
+    import mlpgpu
+
+    L = mlpgpu.lib()
+    h = C.c_void_p()
+    x = np.zeros(8, np.int32)
+    for n in (-1, 0, 3, 4, 16384):
+        assert L.mlp_problem_create_coords(n, x.ctypes.data, x.ctypes.data, 1, 1, C.byref(h)) == 3, n
+        assert b"instance size out of range" in L.mlp_last_error()
+    assert L.mlp_problem_create_coords(10, None, None, 1, 1, C.byref(h)) == 1
+    assert L.mlp_last_error() == b"null argument"
+    assert L.mlp_solver_create(None, 0, C.byref(h)) == 1
+    assert L.mlp_batch_run(None, 31, 10) == 1
+    assert L.mlp_server_create(0, 0, 0, C.byref(h)) == 1
+    assert b"budget" in L.mlp_last_error()

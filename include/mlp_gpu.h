@@ -121,6 +121,11 @@ MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
  * of mlp_solver_dvnd_async). */
 MLP_API int mlp_solver_set_tile_shape(mlp_solver_t s, int32_t shape);
 MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t iterations);
+/* DVND sweep kernel (no counterpart in the reference): 1 (default) the
+ * kernel that reads per-position row and column terms (32-bit solvers that
+ * evaluate all five neighbourhoods), 0 the general fused sweep.  Results are
+ * identical; the switch exists for measurement and testing. */
+MLP_API int mlp_solver_set_sweep_kernel(mlp_solver_t s, int32_t variant);
 /* Candidate mode of every later pass / DVND of this solver.  0 (default): one
  * candidate per reference block (the ODC kernels).  1: TOTAL multi-improvement
  * (the reference's isTotal kernels, source/mlkernel.h:150-163,
@@ -223,7 +228,15 @@ MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape);
  * neighbourhood nb (as mlp_solver_eval) for `tour_dev` (n + 1 entries) over
  * the n x n distances `dist_dev`, writing nb's candidate count of entries to
  * cost_dev / i_dev / j_dev; every pointer is device memory owned by the
- * caller.  All intermediate data lives in one fixed 256 KB device array that
+ * caller.  With size = n + 1 the candidate count is (size + 1) / 2 - 1 for
+ * swap (nb 0), (size + 1) / 2 for 2-opt (nb 1) and size - k - 2 for Or-opt-k
+ * (nb = k + 1).  The tour must hold depot 0 at both ends and every client
+ * 1..n-1 once; it is checked on the device before any distance is read
+ * through it, and a tour that fails yields cost INT64_MIN and i = j = -1 in
+ * every output entry (nothing else is read or written).  Distances are used
+ * only as values: they must be symmetric and in [0, 65535] (as
+ * mlp_problem_from_matrix requires), otherwise the candidates are
+ * meaningless.  All intermediate data lives in one fixed 256 KB device array that
  * the library holds on each GPU it is loaded on until the process exits:
  * n + 1 <= 2048, larger instances are rejected with MLP_ERR_RANGE.  The first
  * call on a device looks up that array's address (make it before any stream
@@ -254,6 +267,8 @@ MLP_API int mlp_batch_set_tile_shape(mlp_batch_t b, int32_t shape);
  * 16 jobs or more, otherwise a six-CTA cluster per job), 1 = cluster, 2 = one
  * CTA per job.  Every mode gives the same results. */
 MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode);
+/* DVND sweep kernel of the batch's iterations (as mlp_solver_set_sweep_kernel). */
+MLP_API int mlp_batch_set_sweep_kernel(mlp_batch_t b, int32_t variant);
 /* Adds a search whose start is MLSolution::random(seed, alpha), built on the
  * device when the batch is (re)started (as mlp_solver_random_tour). */
 MLP_API int mlp_batch_add_random(mlp_batch_t b, mlp_problem_t p, uint32_t seed, float alpha, int32_t* job);

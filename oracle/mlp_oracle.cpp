@@ -11,7 +11,7 @@
  * and start tours are checked against fixtures produced by the reference's
  * compiled CPU evaluator (oracle/_ref, tests/golden/gen_golden.py).
  *
- * Decisions where the reference is not deterministic (documented in the design doc):
+ * Decisions where the reference is not deterministic:
  *   - Per-block winner: argmin over (delta, ctx); the reference's shared-memory
  *     tree depends on blockDim (source/mlkswap.cu:944-964).
  *   - Sort of candidates: stable on (cost, block index); the reference uses

@@ -33,13 +33,16 @@ REF_CUBINS = [os.path.join(REF_DIR, f"ref_{u}.cubin") for u in ("mlkswap", "mlk2
 REF_LAUNCH = os.path.join(REF_DIR, "libref_launch.so")
 
 
-def build_ref() -> Optional[str]:
+def build_ref(ref_src: Optional[str] = None) -> Optional[str]:
     """Compiles the reference's CPU evaluator and its GPU neighbourhood kernels
-    (sm_103a cubins) into _ref/ where the reference sources are mounted, and
-    the launcher of those kernels wherever the cubins are (they travel with
-    the tree); returns the CPU evaluator's path or None."""
-    ref_src = os.environ.get("REF_SRC", "/root/reference/source")
-    if os.path.isdir(ref_src):
+    (sm_103a cubins) into _ref/ from the reference's source/ directory
+    `ref_src` (else the REF_SRC environment variable; skipped when neither is
+    given), and the launcher of those kernels wherever the cubins are (they
+    travel with the tree); returns the CPU evaluator's path or None."""
+    ref_src = ref_src or os.environ.get("REF_SRC")
+    if ref_src and not os.path.isdir(ref_src):
+        raise FileNotFoundError(f"reference sources not found: {ref_src}")
+    if ref_src:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
         subprocess.run(["make", "-s", "-C", HERE, "refgpu", f"REF_SRC={ref_src}"], check=True)
     if all(os.path.exists(c) for c in REF_CUBINS):

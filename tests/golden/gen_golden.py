@@ -3,7 +3,7 @@ evaluator, compiled from the reference sources into oracle/_ref/libmlref.so
 (see oracle/Makefile and oracle/ref_driver.cpp).
 
 Run where the reference tree is mounted:
-    python tests/golden/gen_golden.py [/path/to/reference]
+    python tests/golden/gen_golden.py <reference root>
 
 Outputs
   berlin52.json  instances/01_berlin52.tsp as MLProblem loads it (costTour,
@@ -114,4 +114,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: gen_golden.py <reference root (the directory holding source/ and instances/)>")
+    main(sys.argv[1])

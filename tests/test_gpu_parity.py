@@ -113,6 +113,28 @@ def test_dvnd_local_optimum(mlpgpu_mod, n, seed, wide, clustered):
     assert st["converged"] == 1
 
 
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("n,seed,shape", [(5, 11, 0), (6, 12, 2), (7, 13, 8), (9, 14, 3), (13, 15, 1), (37, 16, 9),
+                                          (64, 17, 6), (97, 18, 7), (130, 19, 5), (257, 20, 4), (611, 21, 2),
+                                          (1000, 22, 3)])
+def test_dvnd_both_sweep_kernels_every_shape(mlpgpu_mod, kernel, n, seed, shape):
+    """The DVND through the general fused sweep (0) and through the term-table
+    sweep (1) equals the oracle's (tour, cost, iterations, moves, evaluations)
+    for tour sizes around every tile edge and each compiled tile shape."""
+    x, y = oracle.clustered_instance(n, seed) if n % 2 else oracle.uniform_instance(n, seed)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, seed)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True))
+    s.set_sweep_kernel(kernel)
+    s.set_tile_shape(shape)
+    s.set_tour(t)
+    st = s.dvnd()
+    ot, ost = oracle.dvnd(t, D)
+    assert np.array_equal(s.tour(), ot)
+    assert (st["cost"], st["iterations"], st["moves"], st["evals"]) == \
+        (ost["cost"], ost["iterations"], ost["moves"], ost["evals"])
+
+
 def test_dvnd_subset_masks_and_iteration_cap(mlpgpu_mod):
     n = 250
     x, y = oracle.uniform_instance(n, 31)

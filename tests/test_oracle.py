@@ -87,9 +87,6 @@ def test_deltas_faithful_fast_bruteforce(n, seed, rnd):
         q = oracle.eval_nb(nb, t, D, faithful=False)
         for a, b in zip(f, q):
             assert np.array_equal(a, b)
-        # every (block, ctx) move: faithful delta == brute force delta
-        for by in range(oracle.num_blocks(nb, size)):
-            pass
     # exhaustive brute force on all moves of every neighbourhood
     for i in range(1, size - 1):
         for j in range(1, size - 1):

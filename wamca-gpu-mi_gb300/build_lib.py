@@ -22,7 +22,7 @@ LIB = os.path.join(LIBDIR, "libmlpgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
-UNITS = ["mlp_kernels.cu", "mlp_total.cu", "mlp_grasp.cu", "mlp_engine.cpp", "mlp_capi.cpp", "mlp_legacy.cpp", "mlp_noalloc.cu",
+UNITS = ["mlp_kernels.cu", "mlp_sweep.cu", "mlp_total.cu", "mlp_grasp.cu", "mlp_engine.cpp", "mlp_capi.cpp", "mlp_legacy.cpp", "mlp_noalloc.cu",
          "mlp_server.cpp"]
 
 

@@ -225,6 +225,11 @@ MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t u) {
   return s->set->set_unroll(u);
 }
 
+MLP_API int mlp_solver_set_sweep_kernel(mlp_solver_t s, int32_t variant) {
+  if (!s) return arg_error("null solver");
+  return s->set->set_sweep_kernel(variant);
+}
+
 MLP_API int mlp_solver_set_total(mlp_solver_t s, int32_t on) {
   if (!s) return arg_error("null solver");
   return s->set->set_total(on != 0);
@@ -726,6 +731,14 @@ MLP_API int mlp_batch_set_merge_mode(mlp_batch_t b, int32_t mode) {
   return kOk;
 }
 
+MLP_API int mlp_batch_set_sweep_kernel(mlp_batch_t b, int32_t variant) {
+  if (!b) return arg_error("null batch");
+  if (variant < 0 || variant > 1) return arg_error("sweep kernel must be 0 or 1");
+  b->sweep_kernel = variant;
+  if (b->set) return b->set->set_sweep_kernel(variant);
+  return kOk;
+}
+
 MLP_API int mlp_batch_set_total(mlp_batch_t b, int32_t on) {
   if (!b) return arg_error("null batch");
   b->total = on != 0;
@@ -786,6 +799,7 @@ static int batch_build(mlp_batch* b) {
   b->set.reset(new JobSet(js, b->wide, b->stream));
   if (b->shape >= 0) MLP_TRY(b->set->set_shape(b->shape));
   MLP_TRY(b->set->set_merge_mode(b->merge_mode));
+  MLP_TRY(b->set->set_sweep_kernel(b->sweep_kernel));
   MLP_TRY(b->set->set_unroll(b->check_interval));
   MLP_TRY(b->set->init());
   MLP_TRY(b->set->set_total(b->total));

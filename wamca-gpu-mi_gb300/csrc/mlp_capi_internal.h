@@ -36,6 +36,7 @@ struct mlp_batch {
   int shape = -1;
   int mask = 0x1f;
   int merge_mode = 0;
+  int sweep_kernel = 1;
   int check_interval = 16;
   bool total = false;
   cudaStream_t own_stream = nullptr;

@@ -287,7 +287,28 @@ struct JobDev {
   int64_t* tkcost;    // kept moves: delta
   uint32_t* tkij;     // kept moves: i | j << 16
   int32_t* tkcount;   // kNumNb kept counts
+  // Row and column terms of the DVND sweep (32-bit jobs; null otherwise):
+  // kTermWords words per position p < size, rebuilt with the prefix arrays.
+  int32_t* RT;
+  int32_t* CT;
 };
+
+// The five deltas of a position pair (r, c), r < c, split into a term of r,
+// a term of c and a few products of the pair's distances (all modulo 2^32).
+// With sz = size, s_p = sz - p, w, W, Q, A the prefix arrays and
+// V_k(p) = W[p+k-1] - W[p] (V_1 = 0, V_2 = w[p+1], V_3 = w[p+1] + w[p+2]):
+//   S(p)    = -s_p w[p] - (s_p - 1) w[p+1]
+//   row r:  RS = S(r);  R2 = -s_r w[r] - 2 Q[r] + (r + 1 + sz) W[r];
+//           RF_k = s_r (A_k[r] - w[r]) - (s_r - k) w[r+k] + (r - sz) V_k(r) - k W[r+k];
+//           RB_k = -s_r w[r] + k W[r];   then -W[r], V_2(r), V_3(r)
+//   col c:  CS = S(c);  C2 = -(s_c - 1) w[c+1] + 2 Q[c] - (c + 1 + sz) W[c];
+//           CF_k = -(s_c - k) w[c+k] + k W[c+k-1];
+//           CB_k = (s_c - k)(A_k[c] - w[c+k]) - s_c w[c] + (c - sz) V_k(c) - k W[c-1];
+//           then W[c], V_2(c), V_3(c)
+// Words: 0 S, 1 R2 / C2, 2..4 RF_k / CF_k, 5..7 RB_k / CB_k, 8 -W[r] / W[c],
+// 9 V_2, 10 V_3, 11 zero.  The sweep's deltas from them are given where it
+// evaluates them (k_sweep_dvnd).
+constexpr int kTermWords = 12;
 
 enum : int {
   kStatCost = 0,       // current cost (int64, or uint32 zero-extended)
@@ -311,5 +332,17 @@ struct SweepTile {
   int32_t L0;
   int32_t pad;
 };
+
+// Tiles of one job's sweep with tl diagonals x tr rows: row blocks start at
+// r0 = 1, 1 + tr, ... <= size - 3, and row block r0 holds the tiles
+// L0 = 1, 1 + tl, ... with r0 + L0 <= size - 2.  Every tile list (the
+// engine's job sets, the allocation-free evaluation) is built from these.
+MLP_HD int sweep_row_blocks(int size, int tr) { return size >= 4 ? (size - 3 + tr - 1) / tr : 0; }
+MLP_HD int sweep_row_tiles(int size, int r0, int tl) { return r0 <= size - 3 ? (size - 2 - r0 + tl - 1) / tl : 0; }
+MLP_HD int sweep_tiles(int size, int tl, int tr) {
+  int c = 0;
+  for (int rb = 0; rb < sweep_row_blocks(size, tr); rb++) c += sweep_row_tiles(size, 1 + rb * tr, tl);
+  return c;
+}
 
 }  // namespace mlp

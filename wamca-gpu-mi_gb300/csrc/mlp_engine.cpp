@@ -262,6 +262,7 @@ size_t job_bytes(int size, bool wide, int moves_cap) {
   b += al(4 * 8);                       // kept_count
   b += al(8 * kStatWords);              // stats
   b += al(4 * (size_t)moves_cap) + al(8 * (size_t)moves_cap);
+  if (!wide) b += al(4 * kTermWords * (size_t)size) * 2;  // RT, CT
   if (merge_needs_ws(size)) b += al(merge_ws_bytes(size));
   return b;
 }
@@ -342,6 +343,11 @@ static void job_layout(Job* j, Problem* p, bool wide, int moves_cap) {
   d.stats = (int64_t*)c;  c += al(8 * kStatWords);
   d.moves_out = moves_cap > 0 ? (uint32_t*)c : nullptr;  c += al(4 * (size_t)moves_cap);
   d.moves_cost = moves_cap > 0 ? (int64_t*)c : nullptr;  c += al(8 * (size_t)moves_cap);
+  d.RT = d.CT = nullptr;
+  if (!wide) {
+    d.RT = (int32_t*)c;  c += al(4 * kTermWords * (size_t)size);
+    d.CT = (int32_t*)c;  c += al(4 * kTermWords * (size_t)size);
+  }
   d.ws = nullptr;
   if (merge_needs_ws(size)) {
     d.ws = (uint8_t*)c;
@@ -357,8 +363,10 @@ static void job_layout(Job* j, Problem* p, bool wide, int moves_cap) {
 void job_tiles(int size, int shape, std::vector<SweepTile>* out) {
   const TileShape ts = kTileShapes[shape];
   out->clear();
-  for (int r0 = 1; r0 <= size - 3; r0 += ts.tr)
-    for (int L0 = 1; r0 + L0 <= size - 2; L0 += ts.tl) out->push_back(SweepTile{0, r0, L0, 0});
+  for (int rb = 0; rb < sweep_row_blocks(size, ts.tr); rb++) {
+    const int r0 = 1 + rb * ts.tr;
+    for (int c = 0; c < sweep_row_tiles(size, r0, ts.tl); c++) out->push_back(SweepTile{0, r0, 1 + c * ts.tl, 0});
+  }
 }
 
 // Tile-shape table chosen by the autotuner (mlpgpu/autotune.py): rows of
@@ -568,8 +576,11 @@ int JobSet::build_tiles() {
   std::vector<SweepTile> tiles;
   for (size_t q = 0; q < jobs_.size(); q++) {
     const int sz = jobs_[q]->size;
-    for (int r0 = 1; r0 <= sz - 3; r0 += ts.tr)
-      for (int L0 = 1; r0 + L0 <= sz - 2; L0 += ts.tl) tiles.push_back(SweepTile{(int32_t)q, r0, L0, 0});
+    for (int rb = 0; rb < sweep_row_blocks(sz, ts.tr); rb++) {
+      const int r0 = 1 + rb * ts.tr;
+      for (int c = 0; c < sweep_row_tiles(sz, r0, ts.tl); c++)
+        tiles.push_back(SweepTile{(int32_t)q, r0, 1 + c * ts.tl, 0});
+    }
   }
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
@@ -652,7 +663,9 @@ int JobSet::set_mask(int mask) {
     int st = ensure_all_active();
     if (st != kOk) return st;
   }
+  const bool was_dvnd = dvnd_sweep();
   mask_ = mask;
+  if (dvnd_sweep() != was_dvnd) drop_graphs();  // the captured sweep kernel changes
   for (size_t q = 0; q < jobs_.size(); q++) {
     jobs_[q]->dev.nb_mask = mask;
     MLP_CUDA(cudaMemcpyAsync(&djobs_[q].nb_mask, &jobs_[q]->dev.nb_mask, sizeof(int32_t),
@@ -727,11 +740,32 @@ int JobSet::launch_iteration() {
     MLP_CUDA(launch_total_finish(djobs_, nj, wide_, solo_smem_, max_size_, stream_), "merge kernel");
     return kOk;
   }
-  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
+  if (dvnd_sweep())
+    MLP_CUDA(launch_sweep_dvnd(dtiles_, ntiles_, djobs_, shape_, stream_), "sweep kernel");
+  else
+    MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
   if (solo_merge())
     MLP_CUDA(launch_merge_solo(djobs_, (int)jobs_.size(), wide_, solo_smem_, max_size_, stream_), "merge kernel");
   else
     MLP_CUDA(launch_merge(djobs_, (int)jobs_.size(), wide_, merge_smem_, max_size_, stream_), "merge kernel");
+  return kOk;
+}
+
+void JobSet::drop_graphs() {
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+  if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
+  loop_graph_ = nullptr;
+}
+
+int JobSet::set_sweep_kernel(int variant) {
+  if (variant < 0 || variant > 1) {
+    set_error("sweep kernel must be 0 (general) or 1 (term tables)");
+    return kErrArg;
+  }
+  if (variant == sweep_variant_) return kOk;
+  sweep_variant_ = variant;
+  drop_graphs();
   return kOk;
 }
 

@@ -162,9 +162,16 @@ class JobSet {
   // candidate (the reference's isTotal kernels), not only each block's best.
   int set_total(bool on);
   bool total() const { return total_; }
+  // DVND sweep kernel: 1 (default) the term-table kernel for 32-bit job sets
+  // that evaluate all five neighbourhoods (k_sweep_dvnd), 0 the general
+  // kernel everywhere.  Both give identical candidates.
+  int set_sweep_kernel(int variant);
+  int sweep_kernel_variant() const { return sweep_variant_; }
 
  private:
   int build_tiles();
+  void drop_graphs();
+  bool dvnd_sweep() const { return sweep_variant_ == 1 && !wide_ && mask_ == 0x1f; }
   int graph_for(int iters, cudaGraphExec_t* out);
   std::vector<Job*> all_jobs_;  // every job of the set (statistics order)
   std::vector<Job*> jobs_;      // the jobs the launches cover
@@ -179,6 +186,7 @@ class JobSet {
   bool solo_smem_ = true;
   int merge_mode_ = 0;
   bool total_ = false;
+  int sweep_variant_ = 1;
   int shape_user_ = -1;  // tile shape to restore when TOTAL mode ends
   JobDev* djobs_ = nullptr;
   SweepTile* dtiles_ = nullptr;

@@ -16,6 +16,13 @@
 // keeps the last call's contents, so calls that overlap on the GPU (on
 // different streams, or from different threads) race and must be serialised
 // by the caller.
+//
+// Inputs: the tour is checked on the device before any distance is read
+// through it (depot 0 at both ends, every client 1..n-1 exactly once).  A tour
+// that fails is replaced by a harmless one for the kernels and every output
+// entry becomes (cost INT64_MIN, i = j = -1).  Distances are only ever used as
+// values, never as addresses; they must be symmetric and in [0, 65535] for the
+// candidates to mean anything.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -41,17 +48,18 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 struct Layout {
-  size_t job, stats, tiles, w, W, Q, A, keys, end;
-  int max_tiles;
+  size_t job, stats, bad, safe, tiles, w, W, Q, A, keys, end;
+  int ntiles;
   __host__ __device__ static size_t al(size_t v) { return (v + 255) / 256 * 256; }
   __host__ __device__ explicit Layout(int size) {
     const size_t pad = (size_t)size + 8;
-    const int rows = (size - 3 + kNaTR - 1) / kNaTR;
-    max_tiles = rows * ((size - 3 + kNaTL - 1) / kNaTL + 1);
+    ntiles = sweep_tiles(size, kNaTL, kNaTR);
     job = 0;
     stats = al(job + sizeof(JobDev));
-    tiles = al(stats + sizeof(int64_t) * kStatWords);
-    w = al(tiles + sizeof(SweepTile) * (size_t)max_tiles);
+    bad = al(stats + sizeof(int64_t) * kStatWords);
+    safe = al(bad + sizeof(int32_t));
+    tiles = al(safe + sizeof(int32_t) * (size_t)size);
+    w = al(tiles + sizeof(SweepTile) * (size_t)ntiles);
     W = al(w + 4 * pad);
     Q = al(W + 8 * pad);
     A = al(Q + 8 * pad);
@@ -60,26 +68,55 @@ struct Layout {
   }
 };
 
-// Writes the job descriptor and the sweep tile list into the scratch array.
-// One CTA: thread rb handles row block rb; a block-wide scan places its tiles.
-__global__ void __launch_bounds__(1024) k_noalloc_setup(unsigned char* base, const int32_t* D, int32_t* tour, int n,
-                                                        int size, int nb, int wide) {
-  __shared__ int s_cnt[1024];
+// Checks the tour and writes the job descriptor and the sweep tile list into
+// the scratch array.  One CTA of kSetupThreads threads: thread rb places the
+// tiles of row block rb (prefix over the row blocks before it).  The tour
+// check marks each client in a shared bitmap; a tour that fails points the
+// descriptor at an identity tour in the scratch array instead, so that no
+// later kernel indexes the distances with an entry of the caller's tour.
+constexpr int kSetupThreads = 256;
+static_assert((kNoAllocMaxSize - 3 + kNaTR - 1) / kNaTR <= kSetupThreads, "one setup thread per row block");
+__global__ void __launch_bounds__(kSetupThreads) k_noalloc_setup(unsigned char* base, const int32_t* D,
+                                                                 const int32_t* tour, int n, int size, int nb,
+                                                                 int wide) {
+  __shared__ int s_cnt[kSetupThreads];
+  __shared__ uint32_t s_seen[kNoAllocMaxSize / 32];
+  __shared__ int s_bad;
   const Layout lay(size);
-  const int rb = threadIdx.x;
-  const int r0 = 1 + rb * kNaTR;
-  int cnt = 0;
-  if (r0 <= size - 3) cnt = (size - 2 - r0 + kNaTL - 1) / kNaTL;  // L0 = 1, 1+TL, ... while r0 + L0 <= size-2
-  s_cnt[rb] = cnt;
+  const int tid = threadIdx.x;
+  for (int q = tid; q < kNoAllocMaxSize / 32; q += blockDim.x) s_seen[q] = 0;
+  if (tid == 0) s_bad = 0;
   __syncthreads();
+  int bad = 0;
+  for (int p = tid; p < size; p += blockDim.x) {
+    const int32_t v = tour[p];
+    if (p == 0 || p == size - 1) {
+      bad |= v != 0;
+    } else if (v < 1 || v >= n) {
+      bad = 1;
+    } else {
+      const uint32_t bit = 1u << (v & 31);
+      bad |= (atomicOr(&s_seen[v >> 5], bit) & bit) != 0;  // client seen before
+    }
+  }
+  if (bad) s_bad = 1;
+  const int rows = sweep_row_blocks(size, kNaTR);
+  const int cnt = tid < rows ? sweep_row_tiles(size, 1 + tid * kNaTR, kNaTL) : 0;
+  s_cnt[tid] = cnt;
+  __syncthreads();
+  const bool ok = s_bad == 0;  // (n - 1 distinct clients in [1, n) and two depots: a permutation)
+  int32_t* safe = (int32_t*)(base + lay.safe);
+  if (!ok)
+    for (int p = tid; p < size; p += blockDim.x) safe[p] = p < size - 1 ? p : 0;
   int off = 0;
-  for (int q = 0; q < rb; q++) off += s_cnt[q];
+  for (int q = 0; q < tid; q++) off += s_cnt[q];
   SweepTile* tiles = (SweepTile*)(base + lay.tiles);
-  for (int c = 0; c < cnt; c++) tiles[off + c] = SweepTile{0, r0, 1 + c * kNaTL, 0};
-  if (rb == 0) {
+  for (int c = 0; c < cnt; c++) tiles[off + c] = SweepTile{0, 1 + tid * kNaTR, 1 + c * kNaTL, 0};
+  if (tid == 0) {
+    *(int32_t*)(base + lay.bad) = ok ? 0 : 1;
     JobDev J{};
     J.D = D;
-    J.tour = tour;
+    J.tour = ok ? const_cast<int32_t*>(tour) : safe;
     J.tour_alt = nullptr;
     J.w = (int32_t*)(base + lay.w);
     J.W = base + lay.W;
@@ -106,8 +143,14 @@ __global__ void k_noalloc_decode(const unsigned char* base, int size, int nb, in
                                  int32_t* oi, int32_t* oj) {
   const Layout lay(size);
   const uint64_t* keys = (const uint64_t*)(base + lay.keys) + nb_offset(nb, size);
+  const bool bad = *(const int32_t*)(base + lay.bad) != 0;
   const int m = nb_blocks(nb, size);
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < m; b += gridDim.x * blockDim.x) {
+    if (bad) {  // the caller's tour failed the check
+      cost[b] = INT64_MIN;
+      oi[b] = oj[b] = -1;
+      continue;
+    }
     const uint64_t k = keys[b];
     if (k == kKeyNone) {
       cost[b] = wide ? INT64_MAX : (int64_t)kCostInfty32;
@@ -174,15 +217,10 @@ extern "C" MLP_API int mlp_eval_noalloc(const int32_t* dist_dev, int32_t n, cons
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const Layout lay(size);
-  // Job descriptor and tile list, then the ADS prefix arrays (which also reset
-  // the candidate keys), then one sweep of neighbourhood nb, then decoding.
-  const int rows = (size - 3 + kNaTR - 1) / kNaTR;
-  if (rows > 1024) {
-    set_error("mlp_eval_noalloc: too many row blocks");
-    return kErrRange;
-  }
-  k_noalloc_setup<<<1, ((rows + 31) / 32) * 32, 0, s>>>(base, dist_dev, const_cast<int32_t*>(tour_dev), n, size,
-                                                         nb, wide ? 1 : 0);
+  // Tour check, job descriptor and tile list, then the ADS prefix arrays
+  // (which also reset the candidate keys), then one sweep of neighbourhood
+  // nb, then decoding.
+  k_noalloc_setup<<<1, kSetupThreads, 0, s>>>(base, dist_dev, tour_dev, n, size, nb, wide ? 1 : 0);
   st = cuda_status(cudaGetLastError(), "noalloc setup kernel");
   if (st != kOk) return st;
   const JobDev* job = reinterpret_cast<const JobDev*>(base + lay.job);
@@ -190,10 +228,7 @@ extern "C" MLP_API int mlp_eval_noalloc(const int32_t* dist_dev, int32_t n, cons
   if (st != kOk) return st;
   st = cuda_status(launch_prepare(job, 1, wide != 0, false, s), "prepare kernel");
   if (st != kOk) return st;
-  // The tile count, from the same formula the setup kernel uses.
-  int ntiles = 0;
-  for (int r0 = 1; r0 <= size - 3; r0 += kNaTR) ntiles += (size - 2 - r0 + kNaTL - 1) / kNaTL;
-  st = cuda_status(launch_sweep(reinterpret_cast<const SweepTile*>(base + lay.tiles), ntiles, job, wide != 0,
+  st = cuda_status(launch_sweep(reinterpret_cast<const SweepTile*>(base + lay.tiles), lay.ntiles, job, wide != 0,
                                 kNoAllocShape, false, s),
                    "sweep kernel");
   if (st != kOk) return st;

@@ -284,8 +284,10 @@ static int server_step(mlp_server* s, int iters) {
   const int nact = (int)s->active.size();
   if (nact > 0 && iters > 0) {
     int ksmall = 0, max_small = 0, max_large = 0, max_size = 0;
+    bool all_nb = true;  // every search evaluates all five neighbourhoods
     for (const Active& a : s->active) {
       const int sz = a.job->size;
+      all_nb &= a.job->dev.nb_mask == 0x1f;
       max_size = std::max(max_size, sz);
       if (sz <= smem_max) {
         ksmall++;
@@ -298,8 +300,7 @@ static int server_step(mlp_server* s, int iters) {
     size_t ntiles = 0;
     for (int q = 0; q < nact; q++) {
       const int sz = s->active[q].job->size;
-      const TileShape ts = kTileShapes[shape];
-      for (int r0 = 1; r0 <= sz - 3; r0 += ts.tr) ntiles += (sz - 2 - r0 + ts.tl - 1) / ts.tl;
+      ntiles += sweep_tiles(sz, kTileShapes[shape].tl, kTileShapes[shape].tr);
     }
     MLP_TRY(ensure_tiles(s, ntiles));
     size_t t = 0;
@@ -316,7 +317,10 @@ static int server_step(mlp_server* s, int iters) {
     MLP_CUDA(cudaMemcpyAsync(s->dtiles, s->htiles, sizeof(SweepTile) * t, cudaMemcpyHostToDevice, s->stream),
              "copy tiles");
     for (int it = 0; it < iters; it++) {
-      MLP_CUDA(launch_sweep(s->dtiles, (int)t, s->djobs, s->wide, shape, true, s->stream), "sweep kernel");
+      if (!s->wide && all_nb)
+        MLP_CUDA(launch_sweep_dvnd(s->dtiles, (int)t, s->djobs, shape, s->stream), "sweep kernel");
+      else
+        MLP_CUDA(launch_sweep(s->dtiles, (int)t, s->djobs, s->wide, shape, true, s->stream), "sweep kernel");
       if (nact >= kSoloMinJobs) {
         MLP_CUDA(launch_merge_solo(s->djobs, ksmall, s->wide, true, max_small, s->stream), "merge kernel");
         MLP_CUDA(launch_merge_solo(s->djobs + ksmall, nact - ksmall, s->wide, false, max_large, s->stream),

@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
         "mlp_solver_set_stream": (C.c_int, [vp, vp]),
         "mlp_solver_set_tile_shape": (C.c_int, [vp, i32]),
         "mlp_solver_set_unroll": (C.c_int, [vp, i32]),
+        "mlp_solver_set_sweep_kernel": (C.c_int, [vp, i32]),
         "mlp_solver_set_total": (C.c_int, [vp, i32]),
         "mlp_solver_eval_oropt": (C.c_int, [vp, i32, vp, vp, vp]),
         "mlp_solver_pass_oropt": (C.c_int, [vp, i32, i32, vp, vp, vp, P(i32), P(i64)]),
@@ -127,6 +128,7 @@ def lib() -> C.CDLL:
         "mlp_batch_set_stream": (C.c_int, [vp, vp]),
         "mlp_batch_set_tile_shape": (C.c_int, [vp, i32]),
         "mlp_batch_set_merge_mode": (C.c_int, [vp, i32]),
+        "mlp_batch_set_sweep_kernel": (C.c_int, [vp, i32]),
         "mlp_batch_set_total": (C.c_int, [vp, i32]),
         "mlp_batch_set_check_interval": (C.c_int, [vp, i32]),
         "mlp_batch_add": (C.c_int, [vp, vp, vp, i32, P(i32)]),
@@ -297,6 +299,11 @@ class Solver:
     def set_unroll(self, u: int) -> None:
         _check(lib().mlp_solver_set_unroll(self._h, u))
 
+    def set_sweep_kernel(self, variant: int) -> None:
+        """DVND sweep kernel: 1 (default) row/column term tables, 0 the
+        general fused sweep; identical results."""
+        _check(lib().mlp_solver_set_sweep_kernel(self._h, variant))
+
     def set_total(self, on: bool = True) -> None:
         """TOTAL multi-improvement (MLKernel isTotal): every evaluated move is a
         merge candidate, not only each reference block's best."""
@@ -459,6 +466,10 @@ class Batch:
     def set_merge_mode(self, mode: int) -> None:
         """0 automatic, 1 six-CTA cluster per job, 2 one CTA per job."""
         _check(lib().mlp_batch_set_merge_mode(self._h, mode))
+
+    def set_sweep_kernel(self, variant: int) -> None:
+        """DVND sweep kernel of the batch (as Solver.set_sweep_kernel)."""
+        _check(lib().mlp_batch_set_sweep_kernel(self._h, variant))
 
     def set_total(self, on: bool = True) -> None:
         """TOTAL candidate mode for every search of the batch (as Solver.set_total)."""

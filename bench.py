@@ -81,6 +81,16 @@ def sweep_bytes(size: int) -> int:
     return sum(blocks(nb, size) * threads(nb, size) * BYTES_PER_EVAL[nb] for nb in range(5))
 
 
+def plain_config(args, world: int = 1) -> dict:
+    """The workload both arms time (identical dicts): the plain n=1000 DVND from
+    the start tours of seeds warmup .. warmup+steps-1 (rank r adds 1000 r)."""
+    return {"workload": "plain DVND n=1000 to local optimum (swap, 2-opt, Or-opt-1/2/3) from seeded random "
+                        "starts, one instance per launch sequence",
+            "n": N_NODES, "instance_seed": INSTANCE_SEED,
+            "start_seeds": [args.warmup, args.warmup + args.steps - 1],
+            "evals_per_sweep": sweep_evals(N_NODES + 1), "replicas": world}
+
+
 def measured_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -88,6 +98,29 @@ def measured_peaks() -> dict:
             d = json.load(f)
         return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
     return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def l2_copy_peak(reps: int = 10, copies: int = 64) -> float:
+    """L2 bandwidth measured here: device copies of an 8 MiB buffer into
+    another (16 MiB read + written, far below the 129 MB L2, warm), `copies`
+    back to back between two CUDA events so that launch gaps are amortised;
+    best of `reps`, in GB/s of bytes read plus written."""
+    import torch
+
+    a = torch.ones(2 << 20, dtype=torch.int32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(8):
+        b.copy_(a)
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = _events(2)
+        e0.record()
+        for _ in range(copies):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3 / copies)
+    return 2 * a.numel() * 4 / best / 1e9
 
 
 def ncu_traffic_per_sweep() -> float | None:
@@ -275,11 +308,12 @@ def run_reference(args, world, rank) -> None:
     x, y = workloads.uniform_instance(n, INSTANCE_SEED)
     D = oracle.dist(x, y, True)
     cores = os.cpu_count() or 1
+    # The GPU arm's start tours: seeds 0 .. warmup-1 warm up, warmup .. warmup+steps-1 are timed.
     for w in range(args.warmup):
-        oracle.dvnd(workloads.random_perm_tour(n, 10_000 + w), D, threads=cores, max_iters=args.ref_iters)
+        oracle.dvnd(workloads.random_perm_tour(n, w), D, threads=cores, max_iters=args.ref_iters)
     times, evals, solves = [], 0, 0
     for k in range(args.steps):
-        t = workloads.random_perm_tour(n, k)
+        t = workloads.random_perm_tour(n, args.warmup + k)
         t0 = time.perf_counter()
         _, st = oracle.dvnd(t, D, threads=cores, max_iters=args.ref_iters)
         times.append(time.perf_counter() - t0)
@@ -292,9 +326,8 @@ def run_reference(args, world, rank) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded uniform coordinates, EUC_2D nint distances)",
-        "config": {"workload": "plain DVND n=1000 (swap, 2-opt, Or-opt-1/2/3) from random starts",
-                   "n": n, "host_threads": cores},
+        "data": "synthetic (seeded uniform coordinates in [0,1000]^2, EUC_2D nint int32 distances)",
+        "config": plain_config(args, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -314,7 +347,9 @@ def _pct(vals, q):
 
 
 def time_sweep(mlpgpu, solver, stream, flush, mask, reps):
-    """Median CUDA-event time of one sweep kernel launch (seconds).
+    """Median CUDA-event time of one sweep kernel launch (seconds), the kernel
+    the solver's DVND iterations run; L2 flushed before each launch unless
+    flush is None (then warm, as inside a DVND).
 
     mlp_solver_sweep(mask, R) enqueues a stats reset, R sweep kernels and a
     prepare; the R = 0 call is timed too and subtracted.
@@ -327,12 +362,14 @@ def time_sweep(mlpgpu, solver, stream, flush, mask, reps):
     a, b, c, d = _events(reps), _events(reps), _events(reps), _events(reps)
     with torch.cuda.stream(stream):
         for r in range(reps):
-            flush.zero_()
+            if flush is not None:
+                flush.zero_()
             a[r].record(stream)
             solver.sweep(mask, 1)
             b[r].record(stream)
         for r in range(reps):
-            flush.zero_()
+            if flush is not None:
+                flush.zero_()
             c[r].record(stream)
             solver.sweep(mask, 0)
             d[r].record(stream)
@@ -365,6 +402,7 @@ def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
     solver.set_tour(tours[0])
     shape = solver.autotune() if args.autotune else None
     t_sweep = time_sweep(mlpgpu, solver, stream, flush, mlpgpu.NB_ALL, args.sweeps)
+    t_sweep_warm = time_sweep(mlpgpu, solver, stream, None, mlpgpu.NB_ALL, args.sweeps)
 
     # DVND steps: device time, start tours already resident in HBM, L2 flushed.
     step_ms, step_evals, step_sweeps, costs = [], [], [], []
@@ -412,7 +450,7 @@ def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
             e2e_evals.append(st.evals)
             assert st.cost == costs[k - args.warmup], "e2e and device runs disagree"
     return {
-        "n": n, "size": size, "t_sweep": t_sweep, "shape": shape, "step_ms": step_ms, "step_evals": step_evals,
+        "n": n, "size": size, "t_sweep": t_sweep, "t_sweep_warm": t_sweep_warm, "shape": shape, "step_ms": step_ms, "step_evals": step_evals,
         "step_sweeps": step_sweeps, "costs": costs, "clocks": clocks, "e2e_s": e2e_s, "e2e_evals": e2e_evals,
     }
 
@@ -503,13 +541,13 @@ def bench_serving(args, mlpgpu, workloads):
         reqs.append((x, y, workloads.random_perm_tour(n, 70_000 + k)))
     out = {"workload": f"{nreq} requests, Poisson arrivals, n log-uniform [50,2000], half uniform / half "
                        "8-cluster coordinates, full DVND each, admission budget 40 GB",
-           "budget_bytes": 40 << 30, "max_active": args.serve_slots, "iters_per_step": args.serve_iters,
-           "rates": []}
+           "requests": nreq, "budget_bytes": 40 << 30, "max_active": args.serve_slots,
+           "iters_per_step": args.serve_iters, "rates": []}
     for rate in [float(r) for r in args.serve_rates.split(",")]:
         srv = mlpgpu.Server(40 << 30, wide=False, max_active=args.serve_slots)
         rng = np.random.default_rng(99)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
-        lat, done, i, rid_n = [], 0, 0, {}
+        lat, lat_n, done, i, rid_n = [], [], 0, 0, {}
         first = last = None
         base = srv.now()
         steps = 0
@@ -526,15 +564,24 @@ def bench_serving(args, mlpgpu, workloads):
                 while srv.now() - base < arrivals[i]:
                     pass
             for rid in srv.finished():
-                _, st, info = srv.result(rid, rid_n.pop(rid))
+                nr = rid_n.pop(rid)
+                _, st, info = srv.result(rid, nr)
                 assert info["status"] == 0, info
                 lat.append(info["finished"] - info["arrival"])
+                lat_n.append(nr)
                 first = info["arrival"] if first is None else min(first, info["arrival"])
                 last = info["finished"] if last is None else max(last, info["finished"])
                 done += 1
         span = last - (base + float(arrivals[0]))
+        by_n = {}
+        for lo, hi in ((0, 200), (200, 800), (800, 1 << 30)):
+            sel = [v for v, m in zip(lat, lat_n) if lo <= m < hi]
+            if sel:
+                by_n[f"n<{hi}" if lo == 0 else (f"n>={lo}" if hi == 1 << 30 else f"{lo}<=n<{hi}")] = {
+                    "count": len(sel), "p50_s": _pct(sel, 0.50), "p99_s": _pct(sel, 0.99)}
         out["rates"].append({"offered_per_s": rate, "solves_per_s": nreq / span, "p50_s": _pct(lat, 0.50),
-                             "p99_s": _pct(lat, 0.99), "mean_s": statistics.mean(lat), "steps": steps})
+                             "p99_s": _pct(lat, 0.99), "mean_s": statistics.mean(lat), "steps": steps,
+                             "by_n": by_n})
         srv.close()
     # Plain per-request form on a sample: build the instance, solve alone.
     import torch
@@ -847,45 +894,82 @@ def run_ours(args, world, rank, local) -> None:
     if rank != 0:
         return
     peaks = measured_peaks()
+    l2_gbs = l2_copy_peak()
     sb = sweep_bytes(size)
     ev = sweep_evals(size)
     achieved = sb / P["t_sweep"] / 1e9
     launches = sum(plain_launches(s) for s in P["step_sweeps"])
     traffic = ncu_traffic_per_sweep()
     step_ms = P["step_ms"]
+    us_iter = 1e3 * sum(step_ms) / sum(P["step_sweeps"])
+    sweep_share = min(1.0, P["t_sweep_warm"] * 1e6 / us_iter)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded uniform coordinates in [0,1000]^2, EUC_2D nint int32 distances)",
-        "config": {"workload": "plain DVND n=1000 to local optimum (swap, 2-opt, Or-opt-1/2/3), one instance "
-                               "per launch sequence, seeded random start per step",
-                   "n": P["n"], "evals_per_sweep": ev, "l2": "flushed (256 MB write) before every timed step",
-                   "tile_shape": P["shape"], "replicas": world,
-                   "loop": "host-checked replays of 16-iteration CUDA graphs"},
+        "config": plain_config(args, world),
+        "method": {"l2": "flushed (256 MB write) before every timed step", "tile_shape": P["shape"],
+                   "loop": "host-checked replays of 16-iteration CUDA graphs",
+                   "timing": "CUDA events on the solver's stream, inputs resident in HBM"},
         "dvnd_solves_per_s": solves,
         "latency_ms": {"p50": _pct(step_ms, 0.50), "p99": _pct(step_ms, 0.99), "mean": statistics.mean(step_ms)},
         "sweeps_per_solve": statistics.mean(P["step_sweeps"]),
-        "us_per_iteration": 1e3 * sum(step_ms) / sum(P["step_sweeps"]),
-        "sweep": {"evals": ev, "us": P["t_sweep"] * 1e6, "evals_per_s": ev / P["t_sweep"]},
+        "us_per_iteration": us_iter,
+        "sweep": {"evals": ev, "us": P["t_sweep"] * 1e6, "us_warm": P["t_sweep_warm"] * 1e6,
+                  "evals_per_s": ev / P["t_sweep"]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": size * 4,
                 "d2h_bytes_per_step": size * 4 + 16 * 8},
-        "roofline": {"kernel": "k_sweep (all five neighbourhoods, n=1000)", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "k_sweep_dvnd (the DVND sweep: all five neighbourhoods, n=1000, one launch)",
+                     "bound": "hbm", "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": traffic, "algorithmic_bytes_per_launch": sb,
-                     "peak_source": peaks["source"] + " hbm_gbs (STREAM copy)"},
+                     "traffic": traffic,
+                     "traffic_source": "profiles/sweep_n1000_ncu.txt (an ncu capture of this kernel, not this run)",
+                     "algorithmic_bytes_per_launch": sb,
+                     "peak_source": peaks["source"] + " hbm_gbs (STREAM copy)",
+                     "l2_peak_gbs": l2_gbs, "frac_l2": achieved / l2_gbs,
+                     "l2_peak_source": "measured in this run: 8 MiB device copies, L2-resident, 64 back to back, best of 10",
+                     "limiter": "l2/issue: D (4 MB) and the tour's arrays stay in L2; DRAM traffic is D once "
+                                "per launch, far below the algorithmic bytes"},
         "clocks": P["clocks"],
         "gpu_launches": launches,
-        "kernel_shares": {"note": "device-time shares of one DVND iteration from the ncu launch list "
-                                  "(profiles/dvnd_n1000_launches.md); the roofline above is the sweep's, the "
-                                  "bandwidth kernel; the merge is latency-bound (critical path of the greedy "
-                                  "rounds and barriers, 0.6 MB of traffic)",
-                          "k_merge": 0.627, "k_sweep": 0.354},
+        "kernel_shares": {"source": "CUDA events in this run: warm DVND sweep launches against DVND iterations",
+                          "k_sweep_dvnd": sweep_share, "k_merge_and_launch_gaps": 1.0 - sweep_share},
     }
     line.update(extra)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(P["n"], budget_s=args.cpu_budget)
+    line["summary"] = summary(line)
     print(json.dumps(line))
+
+
+def summary(line: dict) -> dict:
+    """The line's key results in a few hundred bytes, printed last so that a
+    reader keeping only the line's tail still has them."""
+    out = {"plain_n1000": {"evals_per_s": line["value"], "e2e_evals_per_s": line["e2e"]["value"],
+                           "solves_per_s": line["dvnd_solves_per_s"], "us_per_iteration": line["us_per_iteration"],
+                           "sweep_us": line["sweep"]["us"], "frac_hbm": line["roofline"]["frac"],
+                           "frac_l2": line["roofline"]["frac_l2"]}}
+    b = line.get("batched")
+    if b:
+        out["batched_2048"] = {"speedup_vs_plain": b["speedup_vs_plain"], "solves_per_s": b["solves_per_s"],
+                               "plain_solves_per_s": b["plain_solves_per_s"], "plain_sample": b["plain_sample"],
+                               "seconds": b["seconds"]}
+    s = line.get("serving")
+    if s:
+        out["serving"] = {"requests": s.get("requests"), "plain_solves_per_s": s.get("plain_solves_per_s"),
+                          "rates": [{"offered": r["offered_per_s"], "solves_per_s": r["solves_per_s"],
+                                     "p50_ms": 1e3 * r["p50_s"], "p99_ms": 1e3 * r["p99_s"]} for r in s["rates"]]}
+    g = line.get("large")
+    if g:
+        sw = g["sweep_2opt_oropt3"]
+        out["large_n10000"] = {"sweep_us": sw["us"], "achieved_gbs": sw["achieved_gbs"],
+                               "frac_hbm": sw["achieved_gbs"] / line["roofline"]["peak"],
+                               "dvnd_capped_s": g["dvnd_capped"]["seconds"]}
+    c = line.get("cpu_baseline")
+    if c:
+        out["cpu_baseline_evals_per_s"] = c["value"]
+    return out
 
 
 def main() -> None:

@@ -199,9 +199,10 @@ MLP_API int mlp_solver_dvnd_async(mlp_solver_t s, int32_t nb_mask, int32_t max_i
 MLP_API int mlp_solver_begin(mlp_solver_t s, int32_t nb_mask, int32_t max_iters);
 MLP_API int mlp_solver_enqueue(mlp_solver_t s, int32_t iterations);
 MLP_API int mlp_solver_stats(mlp_solver_t s, mlp_dvnd_stats_t* stats);
-/* Enqueue `repeats` evaluation-only sweeps of nb_mask (timing helper; the tour
- * is not changed): one tiny counter-reset kernel, `repeats` sweep kernels and
- * one ADS rebuild.  *evals_per_sweep = move evaluations of one sweep. */
+/* Enqueue `repeats` sweeps of nb_mask as the solver's DVND iterations run them
+ * (the same kernel, improving candidates only; a timing helper: the tour is
+ * not changed): one tiny counter-reset kernel, `repeats` sweep kernels and one
+ * ADS rebuild.  *evals_per_sweep = move evaluations of one sweep. */
 MLP_API int mlp_solver_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats,
                              int64_t* evals_per_sweep);
 /* Tile-shape table (no counterpart in the reference; chosen by the

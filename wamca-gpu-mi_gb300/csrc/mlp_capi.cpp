@@ -651,9 +651,10 @@ MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape) {
   int best_shape = s->set->shape();
   for (int sh = 0; sh < kNumTileShapes; sh++) {
     MLP_TRY(s->set->set_shape(sh));
-    for (int r = 0; r < 3; r++) MLP_TRY(s->set->sweep_only());
+    MLP_CUDA(launch_stats_begin(s->set->device_jobs(), 1, 1, st), "stats kernel");
+    for (int r = 0; r < 3; r++) MLP_TRY(s->set->sweep_kernel());
     MLP_CUDA(cudaEventRecord(a, st), "event");
-    for (int r = 0; r < 20; r++) MLP_TRY(s->set->sweep_only());
+    for (int r = 0; r < 20; r++) MLP_TRY(s->set->sweep_kernel());
     MLP_CUDA(cudaEventRecord(b, st), "event");
     MLP_CUDA(cudaEventSynchronize(b), "event");
     float ms = 0;

@@ -794,7 +794,10 @@ int JobSet::sweep_only() {
 }
 
 int JobSet::sweep_kernel() {
-  MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, false, stream_), "sweep kernel");
+  if (dvnd_sweep())
+    MLP_CUDA(launch_sweep_dvnd(dtiles_, ntiles_, djobs_, shape_, stream_), "sweep kernel");
+  else
+    MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
   return kOk;
 }
 

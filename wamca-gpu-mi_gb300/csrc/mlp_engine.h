@@ -133,7 +133,8 @@ class JobSet {
   int set_record_moves(bool on);
   // One sweep only (keys left on the device; call prepare() afterwards).
   int sweep_only();
-  // The sweep kernel alone (after a sweep_only() or stats reset).
+  // The sweep kernel of a DVND iteration alone (improving candidates only;
+  // after a statistics reset).
   int sweep_kernel();
   // DVND iterations until every job converged or max_iters sweeps ran.
   int run(int max_iters, bool sync);

@@ -113,8 +113,9 @@ MLP_API int mlp_solver_create(mlp_problem_t p, int32_t wide, mlp_solver_t* out);
 MLP_API void mlp_solver_destroy(mlp_solver_t s);
 /* Stream on which every later call of this solver runs (NULL: the solver's own). */
 MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
-/* Sweep tile shape index (0..9: diagonals x rows = 32x4, 32x8, 32x16, 64x4, 64x8,
- * 64x16, 128x8, 128x16, 32x32, 64x32).  Loop mode of mlp_solver_dvnd: iterations >= 1
+/* Sweep tile shape index (0..13: diagonals x rows = 32x4, 32x8, 32x16, 64x4, 64x8,
+ * 64x16, 128x8, 128x16, 32x32, 64x32, then 64x8, 64x16, 64x32, 128x16 where the
+ * DVND sweep gives each thread two adjacent diagonals).  Loop mode of mlp_solver_dvnd: iterations >= 1
  * (default 16) replays CUDA graphs of that many iterations and checks
  * convergence on the host in between; iterations = 0 runs the whole loop on
  * the device (a CUDA-graph while node, no host round trips; always the mode

@@ -102,7 +102,7 @@ def test_tuning_table_set_get_load_and_validation(tmp_path):
                                  "timings": [{"n": 200, "one_s": {"0": 0.1}}]}, indent=1))
         assert mlpgpu.lib().mlp_tuning_load(str(p).encode()) == 0
         assert mlpgpu.tuning_table() == [(201, 1, 2), (5001, 3, 7)]
-        for bad in ([(101, 0, 10)], [(1001, 0, 1), (101, 0, 1)], [(0, 0, 0)]):
+        for bad in ([(101, 0, 14)], [(1001, 0, 1), (101, 0, 1)], [(0, 0, 0)]):
             with pytest.raises(mlpgpu.MLPError):
                 mlpgpu.set_tuning_table(bad)
         assert mlpgpu.tuning_table() == [(201, 1, 2), (5001, 3, 7)]  # unchanged by rejected tables

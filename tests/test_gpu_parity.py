@@ -116,7 +116,8 @@ def test_dvnd_local_optimum(mlpgpu_mod, n, seed, wide, clustered):
 @pytest.mark.parametrize("kernel", [0, 1])
 @pytest.mark.parametrize("n,seed,shape", [(5, 11, 0), (6, 12, 2), (7, 13, 8), (9, 14, 3), (13, 15, 1), (37, 16, 9),
                                           (64, 17, 6), (97, 18, 7), (130, 19, 5), (257, 20, 4), (611, 21, 2),
-                                          (1000, 22, 3)])
+                                          (1000, 22, 3), (5, 23, 10), (8, 24, 11), (11, 25, 12), (66, 26, 13),
+                                          (70, 27, 10), (131, 28, 11), (199, 29, 12), (402, 30, 13), (777, 31, 11)])
 def test_dvnd_both_sweep_kernels_every_shape(mlpgpu_mod, kernel, n, seed, shape):
     """The DVND through the general fused sweep (0) and through the term-table
     sweep (1) equals the oracle's (tour, cost, iterations, moves, evaluations)

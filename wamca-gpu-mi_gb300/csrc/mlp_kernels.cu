@@ -1707,6 +1707,11 @@ cudaError_t sweep_dispatch(const SweepTile* tiles, int ntiles, const JobDev* job
     case 7: return sweep_launch<WIDE, 128, 16>(tiles, ntiles, jobs, improve_only, s);
     case 8: return sweep_launch<WIDE, 32, 32>(tiles, ntiles, jobs, improve_only, s);
     case 9: return sweep_launch<WIDE, 64, 32>(tiles, ntiles, jobs, improve_only, s);
+    // Two-diagonals-per-thread shapes of the DVND sweep: here one per thread.
+    case 10: return sweep_launch<WIDE, 64, 8>(tiles, ntiles, jobs, improve_only, s);
+    case 11: return sweep_launch<WIDE, 64, 16>(tiles, ntiles, jobs, improve_only, s);
+    case 12: return sweep_launch<WIDE, 64, 32>(tiles, ntiles, jobs, improve_only, s);
+    case 13: return sweep_launch<WIDE, 128, 16>(tiles, ntiles, jobs, improve_only, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -7,13 +7,17 @@
 
 namespace mlp {
 
-// Sweep tile shapes (diagonals x rows) compiled into the library.
+// Sweep tile shapes (diagonals x rows) compiled into the library.  per = 2:
+// the DVND sweep gives each thread two adjacent diagonals (k_sweep_dvnd2);
+// every other sweep kernel runs such a shape with one diagonal per thread.
 struct TileShape {
-  int tl;  // diagonals per tile (= threads per CTA)
-  int tr;  // rows per tile
+  int tl;   // diagonals per tile
+  int tr;   // rows per tile
+  int per;  // diagonals per thread of the DVND sweep
 };
-constexpr TileShape kTileShapes[] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {64, 16}, {128, 8}, {128, 16},
-                                       {32, 32}, {64, 32}};
+constexpr TileShape kTileShapes[] = {{32, 4, 1},  {32, 8, 1},  {32, 16, 1}, {64, 4, 1},  {64, 8, 1},
+                                       {64, 16, 1}, {128, 8, 1}, {128, 16, 1}, {32, 32, 1}, {64, 32, 1},
+                                       {64, 8, 2},  {64, 16, 2}, {64, 32, 2},  {128, 16, 2}};
 constexpr int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
 
 // Bytes of dynamic shared memory the merge kernel needs for `size`

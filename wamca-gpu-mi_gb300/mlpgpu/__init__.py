@@ -25,6 +25,11 @@ TUNING_PATH = os.path.join(_HERE, "tuning_gb300.json")
 
 NB_SWAP, NB_2OPT, NB_OROPT1, NB_OROPT2, NB_OROPT3 = range(5)
 NB_ALL = 0x1F
+# Compiled sweep tile shapes (diagonals x rows; the last four give the DVND
+# sweep two diagonals per thread), indices 0 .. NUM_TILE_SHAPES - 1.
+TILE_SHAPES = ((32, 4), (32, 8), (32, 16), (64, 4), (64, 8), (64, 16), (128, 8), (128, 16), (32, 32), (64, 32),
+               (64, 8), (64, 16), (64, 32), (128, 16))
+NUM_TILE_SHAPES = len(TILE_SHAPES)
 NB_NAMES = ("swap", "2opt", "oropt1", "oropt2", "oropt3")
 
 

@@ -39,7 +39,7 @@ def _best(times: dict) -> int:
     return min(times, key=times.get)
 
 
-def time_one(n: int, shapes=range(10), iters: int = 24, reps: int = 3) -> dict:
+def time_one(n: int, shapes=range(mlpgpu.NUM_TILE_SHAPES), iters: int = 24, reps: int = 3) -> dict:
     """Seconds of `iters` DVND iterations of one job of n nodes, per shape."""
     x, y = workloads.uniform_instance(n, 7)
     p = mlpgpu.Problem.from_coords(x, y)
@@ -60,7 +60,7 @@ def time_one(n: int, shapes=range(10), iters: int = 24, reps: int = 3) -> dict:
     return out
 
 
-def time_many(n: int, shapes=range(10), iters: int = 12, reps: int = 2) -> dict:
+def time_many(n: int, shapes=range(mlpgpu.NUM_TILE_SHAPES), iters: int = 12, reps: int = 2) -> dict:
     """Seconds of `iters` DVND iterations of a batch of many jobs of n nodes, per shape."""
     jobs = int(min(256, max(8, 3e8 // (n * n))))
     x, y = workloads.clustered_instance(n, 11)
@@ -101,7 +101,9 @@ def tune(sizes=DEFAULT_SIZES, verbose: bool = True) -> dict:
         dev = torch.cuda.get_device_name(0)
     except Exception:
         pass
-    return {"device": dev, "shapes": "0..9 = 32x4, 32x8, 32x16, 64x4, 64x8, 64x16, 128x8, 128x16, 32x32, 64x32 (diagonals x rows)",
+    return {"device": dev, "shapes": "0..13 = 32x4, 32x8, 32x16, 64x4, 64x8, 64x16, 128x8, 128x16, 32x32, 64x32 "
+                                      "(diagonals x rows), then 64x8, 64x16, 64x32, 128x16 with two diagonals per "
+                                      "thread in the DVND sweep",
             "table": rows, "timings": detail}
 
 

@@ -989,8 +989,8 @@ def main() -> None:
                     help="extra workloads reported beside the plain n=1000 headline")
     ap.add_argument("--batch-instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=128)
-    ap.add_argument("--serve-requests", type=int, default=2000)
-    ap.add_argument("--serve-rates", default="250,500,1000")
+    ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--serve-rates", default="250,500,1000,1500,2000,3000")
     ap.add_argument("--serve-slots", type=int, default=1024)
     ap.add_argument("--serve-iters", type=int, default=2)
     ap.add_argument("--large-n", type=int, default=10000)

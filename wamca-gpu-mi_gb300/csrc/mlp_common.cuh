@@ -310,6 +310,35 @@ struct JobDev {
 // evaluates them (k_sweep_dvnd).
 constexpr int kTermWords = 12;
 
+#ifdef __CUDACC__
+// Inputs of position p's terms: w[p..p+3] (zero at and beyond size), W[p],
+// Q[p] and A_k[p], all modulo 2^32.
+struct TermIn {
+  uint32_t w0, w1, w2, w3, W, Q, A1, A2, A3;
+};
+__device__ __forceinline__ void row_terms(const TermIn& x, int p, int sz, int4& o0, int4& o1, int4& o2) {
+  const uint32_t up = (uint32_t)p, usz = (uint32_t)sz, sp = usz - up, upsz = up - usz;
+  const uint32_t W1 = x.W + x.w1, W2 = W1 + x.w2, W3 = W2 + x.w3, V2 = x.w1, V3 = x.w1 + x.w2;
+  const uint32_t S = 0u - sp * x.w0 - (sp - 1u) * x.w1, RB0 = 0u - sp * x.w0;
+  o0 = make_int4((int)S, (int)(RB0 - 2u * x.Q + (up + 1u + usz) * x.W), (int)(sp * (x.A1 - x.w0) - (sp - 1u) * x.w1 - W1),
+                 (int)(sp * (x.A2 - x.w0) - (sp - 2u) * x.w2 + upsz * V2 - 2u * W2));
+  o1 = make_int4((int)(sp * (x.A3 - x.w0) - (sp - 3u) * x.w3 + upsz * V3 - 3u * W3), (int)(RB0 + x.W),
+                 (int)(RB0 + 2u * x.W), (int)(RB0 + 3u * x.W));
+  o2 = make_int4((int)(0u - x.W), (int)V2, (int)V3, 0);
+}
+__device__ __forceinline__ void col_terms(const TermIn& x, int p, int sz, int4& o0, int4& o1, int4& o2) {
+  const uint32_t up = (uint32_t)p, usz = (uint32_t)sz, sp = usz - up, upsz = up - usz;
+  const uint32_t Wm1 = x.W - x.w0, W1 = x.W + x.w1, W2 = W1 + x.w2, V2 = x.w1, V3 = x.w1 + x.w2;
+  const uint32_t S = 0u - sp * x.w0 - (sp - 1u) * x.w1, RB0 = 0u - sp * x.w0;
+  o0 = make_int4((int)S, (int)(0u - (sp - 1u) * x.w1 + 2u * x.Q - (up + 1u + usz) * x.W),
+                 (int)(0u - (sp - 1u) * x.w1 + x.W), (int)(0u - (sp - 2u) * x.w2 + 2u * W1));
+  o1 = make_int4((int)(0u - (sp - 3u) * x.w3 + 3u * W2), (int)((sp - 1u) * (x.A1 - x.w1) + RB0 - Wm1),
+                 (int)((sp - 2u) * (x.A2 - x.w2) + RB0 + upsz * V2 - 2u * Wm1),
+                 (int)((sp - 3u) * (x.A3 - x.w3) + RB0 + upsz * V3 - 3u * Wm1));
+  o2 = make_int4((int)x.W, (int)V2, (int)V3, 0);
+}
+#endif
+
 enum : int {
   kStatCost = 0,       // current cost (int64, or uint32 zero-extended)
   kStatIters = 1,      // iterations that applied moves

@@ -345,8 +345,8 @@ static void job_layout(Job* j, Problem* p, bool wide, int moves_cap) {
   d.moves_cost = moves_cap > 0 ? (int64_t*)c : nullptr;  c += al(8 * (size_t)moves_cap);
   d.RT = d.CT = nullptr;
   if (!wide) {
-    d.RT = (int32_t*)c;  c += al(4 * kTermWords * (size_t)size);
-    d.CT = (int32_t*)c;  c += al(4 * kTermWords * (size_t)size);
+    d.RT = j->rt_mem = (int32_t*)c;  c += al(4 * kTermWords * (size_t)size);
+    d.CT = j->ct_mem = (int32_t*)c;  c += al(4 * kTermWords * (size_t)size);
   }
   d.ws = nullptr;
   if (merge_needs_ws(size)) {
@@ -562,6 +562,8 @@ int JobSet::init() {
   std::vector<JobDev> h(jobs_.size());
   for (size_t q = 0; q < jobs_.size(); q++) {
     jobs_[q]->dev.stats = dstats_ + q * kStatWords;
+    jobs_[q]->dev.RT = local_terms() ? nullptr : jobs_[q]->rt_mem;
+    jobs_[q]->dev.CT = local_terms() ? nullptr : jobs_[q]->ct_mem;
     h[q] = jobs_[q]->dev;
   }
   MLP_CUDA(cudaMemcpyAsync(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice, stream_),
@@ -741,7 +743,7 @@ int JobSet::launch_iteration() {
     return kOk;
   }
   if (dvnd_sweep())
-    MLP_CUDA(launch_sweep_dvnd(dtiles_, ntiles_, djobs_, shape_, stream_), "sweep kernel");
+    MLP_CUDA(launch_sweep_dvnd(dtiles_, ntiles_, djobs_, shape_, local_terms(), stream_), "sweep kernel");
   else
     MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
   if (solo_merge())
@@ -795,7 +797,7 @@ int JobSet::sweep_only() {
 
 int JobSet::sweep_kernel() {
   if (dvnd_sweep())
-    MLP_CUDA(launch_sweep_dvnd(dtiles_, ntiles_, djobs_, shape_, stream_), "sweep kernel");
+    MLP_CUDA(launch_sweep_dvnd(dtiles_, ntiles_, djobs_, shape_, local_terms(), stream_), "sweep kernel");
   else
     MLP_CUDA(launch_sweep(dtiles_, ntiles_, djobs_, wide_, shape_, true, stream_), "sweep kernel");
   return kOk;

@@ -83,6 +83,8 @@ struct Job {
   bool async_alloc = false;
   void* total = nullptr;  // TOTAL lists (allocated when a job set first enters TOTAL mode)
   size_t total_bytes = 0;
+  int32_t* rt_mem = nullptr;  // the arena's term tables (32-bit jobs); dev.RT/CT point
+  int32_t* ct_mem = nullptr;  // at them unless the job's set computes terms per tile
   ~Job();
 };
 
@@ -173,6 +175,10 @@ class JobSet {
   int build_tiles();
   void drop_graphs();
   bool dvnd_sweep() const { return sweep_variant_ == 1 && !wide_ && mask_ == 0x1f; }
+  // A set of one search computes the DVND sweep's row and column terms in
+  // every tile instead of having the ADS rebuild (one CTA, on the merge's
+  // critical path) write term tables.
+  bool local_terms() const { return all_jobs_.size() == 1; }
   int graph_for(int iters, cudaGraphExec_t* out);
   std::vector<Job*> all_jobs_;  // every job of the set (statistics order)
   std::vector<Job*> jobs_;      // the jobs the launches cover

@@ -132,35 +132,20 @@ __device__ void block_exclusive_scan3(T a, T b, T c, T* sa, T* sb, T* sc, T& ea,
 // w (w_s: the job's sz weights), W[p], Q[p] and A; 32-bit modular arithmetic.
 __device__ __forceinline__ void write_terms(const JobDev* J, int p, int sz, const int32_t* w_s, uint32_t Wp,
                                             uint32_t Qp, const int32_t* A, int pad) {
-  const uint32_t w0 = (uint32_t)w_s[p];
-  const uint32_t w1 = p + 1 < sz ? (uint32_t)w_s[p + 1] : 0u;
-  const uint32_t w2 = p + 2 < sz ? (uint32_t)w_s[p + 2] : 0u;
-  const uint32_t w3 = p + 3 < sz ? (uint32_t)w_s[p + 3] : 0u;
-  const uint32_t up = (uint32_t)p, usz = (uint32_t)sz, sp = usz - up;
-  const uint32_t Wm1 = Wp - w0, W1 = Wp + w1, W2 = W1 + w2, W3 = W2 + w3;
-  const uint32_t A1 = (uint32_t)A[p], A2 = (uint32_t)A[pad + p], A3 = (uint32_t)A[2 * pad + p];
-  const uint32_t V2 = w1, V3 = w1 + w2, S = 0u - sp * w0 - (sp - 1u) * w1;
-  const uint32_t upsz = up - usz;  // p - sz
+  TermIn x;
+  x.w0 = (uint32_t)w_s[p];
+  x.w1 = p + 1 < sz ? (uint32_t)w_s[p + 1] : 0u;
+  x.w2 = p + 2 < sz ? (uint32_t)w_s[p + 2] : 0u;
+  x.w3 = p + 3 < sz ? (uint32_t)w_s[p + 3] : 0u;
+  x.W = Wp;
+  x.Q = Qp;
+  x.A1 = (uint32_t)A[p];
+  x.A2 = (uint32_t)A[pad + p];
+  x.A3 = (uint32_t)A[2 * pad + p];
   int4* rt = reinterpret_cast<int4*>(J->RT + (size_t)p * kTermWords);
   int4* ct = reinterpret_cast<int4*>(J->CT + (size_t)p * kTermWords);
-  const uint32_t R2 = 0u - sp * w0 - 2u * Qp + (up + 1u + usz) * Wp;
-  const uint32_t RF1 = sp * (A1 - w0) - (sp - 1u) * w1 - W1;
-  const uint32_t RF2 = sp * (A2 - w0) - (sp - 2u) * w2 + upsz * V2 - 2u * W2;
-  const uint32_t RF3 = sp * (A3 - w0) - (sp - 3u) * w3 + upsz * V3 - 3u * W3;
-  const uint32_t RB0 = 0u - sp * w0;
-  rt[0] = make_int4((int)S, (int)R2, (int)RF1, (int)RF2);
-  rt[1] = make_int4((int)RF3, (int)(RB0 + Wp), (int)(RB0 + 2u * Wp), (int)(RB0 + 3u * Wp));
-  rt[2] = make_int4((int)(0u - Wp), (int)V2, (int)V3, 0);
-  const uint32_t C2 = 0u - (sp - 1u) * w1 + 2u * Qp - (up + 1u + usz) * Wp;
-  const uint32_t CF1 = 0u - (sp - 1u) * w1 + Wp;
-  const uint32_t CF2 = 0u - (sp - 2u) * w2 + 2u * W1;
-  const uint32_t CF3 = 0u - (sp - 3u) * w3 + 3u * W2;
-  const uint32_t CB1 = (sp - 1u) * (A1 - w1) + RB0 - Wm1;
-  const uint32_t CB2 = (sp - 2u) * (A2 - w2) + RB0 + upsz * V2 - 2u * Wm1;
-  const uint32_t CB3 = (sp - 3u) * (A3 - w3) + RB0 + upsz * V3 - 3u * Wm1;
-  ct[0] = make_int4((int)S, (int)C2, (int)CF1, (int)CF2);
-  ct[1] = make_int4((int)CF3, (int)CB1, (int)CB2, (int)CB3);
-  ct[2] = make_int4((int)Wp, (int)V2, (int)V3, 0);
+  row_terms(x, p, sz, rt[0], rt[1], rt[2]);
+  col_terms(x, p, sz, ct[0], ct[1], ct[2]);
 }
 
 // --------------------------------------------------------------------------

@@ -68,10 +68,13 @@ cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use
 constexpr int kTotalShapeSmall = 3;  // 64 diagonals x 4 rows: sets whose tours have <= 2000 positions
 constexpr int kTotalShapeLarge = 7;  // 128 diagonals x 16 rows
 inline int total_shape(int max_size) { return max_size <= 2000 ? kTotalShapeSmall : kTotalShapeLarge; }
-// DVND sweep of 32-bit jobs over all five neighbourhoods from the jobs' row
-// and column term tables (mlp_sweep.cu): the same keys as launch_sweep with
-// improve_only for jobs whose mask is all five neighbourhoods.
-cudaError_t launch_sweep_dvnd(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape, cudaStream_t s);
+// DVND sweep of 32-bit jobs over all five neighbourhoods (mlp_sweep.cu): the
+// same keys as launch_sweep with improve_only for jobs whose mask is all five
+// neighbourhoods.  local = false: the terms come from the jobs' term tables
+// (written by the ADS rebuild); local = true: every tile computes its own from
+// the prefix arrays (jobs whose descriptors carry no tables).
+cudaError_t launch_sweep_dvnd(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape, bool local,
+                              cudaStream_t s);
 cudaError_t launch_sweep_collect(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool wide, int shape,
                                  cudaStream_t s);
 cudaError_t launch_total_select(const JobDev* jobs, int njobs, bool wide, cudaStream_t s);

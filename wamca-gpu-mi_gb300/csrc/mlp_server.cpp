@@ -318,7 +318,7 @@ static int server_step(mlp_server* s, int iters) {
              "copy tiles");
     for (int it = 0; it < iters; it++) {
       if (!s->wide && all_nb)
-        MLP_CUDA(launch_sweep_dvnd(s->dtiles, (int)t, s->djobs, shape, s->stream), "sweep kernel");
+        MLP_CUDA(launch_sweep_dvnd(s->dtiles, (int)t, s->djobs, shape, false, s->stream), "sweep kernel");
       else
         MLP_CUDA(launch_sweep(s->dtiles, (int)t, s->djobs, s->wide, shape, true, s->stream), "sweep kernel");
       if (nact >= kSoloMinJobs) {

@@ -62,7 +62,10 @@ __device__ __forceinline__ void publish_diagonal(uint64_t* keys, int sz, int r0,
 // diagonal L = L0 + tid (c = r + L).  Distances E(x, y) = D[t[x]][t[y]] are
 // staged in skewed layout sS[a][b] = E(r0 - 1 + a, r0 - 1 + a + L0 - 1 + b);
 // row a (1-based) is r = r0 + a - 1, and thread tid reads column b = tid + 1.
-template <int TL, int TR>
+// LOCAL: the tile computes its rows' and columns' terms from the prefix arrays
+// itself (a job set of one search: the ADS rebuild, on one SM, then writes no
+// term tables; here the work is spread over every tile).
+template <int TL, int TR, bool LOCAL>
 __global__ void __launch_bounds__(TL) k_sweep_dvnd(const SweepTile* __restrict__ tiles,
                                                    const JobDev* __restrict__ jobs) {
   constexpr int SR = TR + 3, SC = TL + 3, NT = TR + TL + 5, NCS = TL + TR - 1;
@@ -86,9 +89,7 @@ __global__ void __launch_bounds__(TL) k_sweep_dvnd(const SweepTile* __restrict__
     // Tour entries of the tile's rows and columns and the term words of its
     // rows and columns: every load issued before any store.
     constexpr int kSR = (SR + TL - 1) / TL, kNT = (NT + TL - 1) / TL;
-    constexpr int kR = (3 * TR + TL - 1) / TL, kC = (3 * NCS + TL - 1) / TL;
     int32_t vRT[kSR], vCT[kNT];
-    int4 vR[kR], vC[kC];
 #pragma unroll
     for (int u = 0; u < kSR; u++) {
       const int q = tid + u * TL, p = r0 - 1 + q;
@@ -99,15 +100,66 @@ __global__ void __launch_bounds__(TL) k_sweep_dvnd(const SweepTile* __restrict__
       const int q = tid + u * TL, p = r0 + L0 - 2 + q;
       vCT[u] = (q < NT && p <= sz - 1) ? t[p] : 0;
     }
+    if constexpr (LOCAL) {
+      // Term inputs of the tile's TR rows and NCS columns (struct s < TR: row
+      // r0 + s; else column r0 + L0 + s - TR), then the terms themselves.
+      constexpr int kS = (TR + NCS + TL - 1) / TL;
+      const int32_t* __restrict__ w = J->w;
+      const uint32_t* __restrict__ Wg = (const uint32_t*)J->W;
+      const uint32_t* __restrict__ Qg = (const uint32_t*)J->Q;
+      const int32_t* __restrict__ Ag = J->A;
+      const int pad = sz + 8;
+      TermIn xin[kS];
 #pragma unroll
-    for (int u = 0; u < kR; u++) {
-      const int q = tid + u * TL, p = r0 + q / 3;
-      vR[u] = (q < 3 * TR && p <= sz - 1) ? __ldg(RT + (size_t)p * 3 + q % 3) : make_int4(0, 0, 0, 0);
-    }
+      for (int u = 0; u < kS; u++) {
+        const int s = tid + u * TL, p = s < TR ? r0 + s : r0 + L0 + (s - TR);
+        TermIn x{};
+        if (s < TR + NCS && p <= sz - 1) {
+          x.w0 = (uint32_t)w[p];
+          x.w1 = (uint32_t)w[p + 1];  // zero at and beyond sz (arrays padded to sz + 8)
+          x.w2 = (uint32_t)w[p + 2];
+          x.w3 = (uint32_t)w[p + 3];
+          x.W = Wg[p];
+          x.Q = Qg[p];
+          x.A1 = (uint32_t)Ag[p];
+          x.A2 = (uint32_t)Ag[pad + p];
+          x.A3 = (uint32_t)Ag[2 * pad + p];
+        }
+        xin[u] = x;
+      }
 #pragma unroll
-    for (int u = 0; u < kC; u++) {
-      const int q = tid + u * TL, p = r0 + L0 + q / 3;
-      vC[u] = (q < 3 * NCS && p <= sz - 1) ? __ldg(CT + (size_t)p * 3 + q % 3) : make_int4(0, 0, 0, 0);
+      for (int u = 0; u < kS; u++) {
+        const int s = tid + u * TL;
+        if (s < TR) {
+          row_terms(xin[u], r0 + s, sz, sRt[s][0], sRt[s][1], sRt[s][2]);
+        } else if (s < TR + NCS) {
+          const int q = s - TR;
+          col_terms(xin[u], r0 + L0 + q, sz, sCt[q][0], sCt[q][1], sCt[q][2]);
+        }
+      }
+    } else {
+      constexpr int kR = (3 * TR + TL - 1) / TL, kC = (3 * NCS + TL - 1) / TL;
+      int4 vR[kR], vC[kC];
+#pragma unroll
+      for (int u = 0; u < kR; u++) {
+        const int q = tid + u * TL, p = r0 + q / 3;
+        vR[u] = (q < 3 * TR && p <= sz - 1) ? __ldg(RT + (size_t)p * 3 + q % 3) : make_int4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int u = 0; u < kC; u++) {
+        const int q = tid + u * TL, p = r0 + L0 + q / 3;
+        vC[u] = (q < 3 * NCS && p <= sz - 1) ? __ldg(CT + (size_t)p * 3 + q % 3) : make_int4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int u = 0; u < kR; u++) {
+        const int q = tid + u * TL;
+        if (q < 3 * TR) sRt[q / 3][q % 3] = vR[u];
+      }
+#pragma unroll
+      for (int u = 0; u < kC; u++) {
+        const int q = tid + u * TL;
+        if (q < 3 * NCS) sCt[q / 3][q % 3] = vC[u];
+      }
     }
 #pragma unroll
     for (int u = 0; u < kSR; u++) {
@@ -118,16 +170,6 @@ __global__ void __launch_bounds__(TL) k_sweep_dvnd(const SweepTile* __restrict__
     for (int u = 0; u < kNT; u++) {
       const int q = tid + u * TL;
       if (q < NT) sColT[q] = vCT[u];
-    }
-#pragma unroll
-    for (int u = 0; u < kR; u++) {
-      const int q = tid + u * TL;
-      if (q < 3 * TR) sRt[q / 3][q % 3] = vR[u];
-    }
-#pragma unroll
-    for (int u = 0; u < kC; u++) {
-      const int q = tid + u * TL;
-      if (q < 3 * NCS) sCt[q / 3][q % 3] = vC[u];
     }
   }
   __syncthreads();
@@ -498,8 +540,9 @@ __global__ void __launch_bounds__(TLD / 2) k_sweep_dvnd2(const SweepTile* __rest
 }
 
 template <int TL, int TR>
-cudaError_t sweep_dvnd_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, cudaStream_t s) {
-  k_sweep_dvnd<TL, TR><<<ntiles, TL, 0, s>>>(tiles, jobs);
+cudaError_t sweep_dvnd_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool local, cudaStream_t s) {
+  if (local) k_sweep_dvnd<TL, TR, true><<<ntiles, TL, 0, s>>>(tiles, jobs);
+  else k_sweep_dvnd<TL, TR, false><<<ntiles, TL, 0, s>>>(tiles, jobs);
   return cudaGetLastError();
 }
 
@@ -511,23 +554,30 @@ cudaError_t sweep_dvnd2_launch(const SweepTile* tiles, int ntiles, const JobDev*
   return cudaGetLastError();
 }
 
-cudaError_t launch_sweep_dvnd(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape, cudaStream_t s) {
+cudaError_t launch_sweep_dvnd(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape, bool local,
+                              cudaStream_t s) {
   if (ntiles <= 0) return cudaSuccess;
   switch (shape) {
-    case 0: return sweep_dvnd_launch<32, 4>(tiles, ntiles, jobs, s);
-    case 1: return sweep_dvnd_launch<32, 8>(tiles, ntiles, jobs, s);
-    case 2: return sweep_dvnd_launch<32, 16>(tiles, ntiles, jobs, s);
-    case 3: return sweep_dvnd_launch<64, 4>(tiles, ntiles, jobs, s);
-    case 4: return sweep_dvnd_launch<64, 8>(tiles, ntiles, jobs, s);
-    case 5: return sweep_dvnd_launch<64, 16>(tiles, ntiles, jobs, s);
-    case 6: return sweep_dvnd_launch<128, 8>(tiles, ntiles, jobs, s);
-    case 7: return sweep_dvnd_launch<128, 16>(tiles, ntiles, jobs, s);
-    case 8: return sweep_dvnd_launch<32, 32>(tiles, ntiles, jobs, s);
-    case 9: return sweep_dvnd_launch<64, 32>(tiles, ntiles, jobs, s);
-    case 10: return sweep_dvnd2_launch<64, 8>(tiles, ntiles, jobs, s);
-    case 11: return sweep_dvnd2_launch<64, 16>(tiles, ntiles, jobs, s);
-    case 12: return sweep_dvnd2_launch<64, 32>(tiles, ntiles, jobs, s);
-    case 13: return sweep_dvnd2_launch<128, 16>(tiles, ntiles, jobs, s);
+    case 0: return sweep_dvnd_launch<32, 4>(tiles, ntiles, jobs, local, s);
+    case 1: return sweep_dvnd_launch<32, 8>(tiles, ntiles, jobs, local, s);
+    case 2: return sweep_dvnd_launch<32, 16>(tiles, ntiles, jobs, local, s);
+    case 3: return sweep_dvnd_launch<64, 4>(tiles, ntiles, jobs, local, s);
+    case 4: return sweep_dvnd_launch<64, 8>(tiles, ntiles, jobs, local, s);
+    case 5: return sweep_dvnd_launch<64, 16>(tiles, ntiles, jobs, local, s);
+    case 6: return sweep_dvnd_launch<128, 8>(tiles, ntiles, jobs, local, s);
+    case 7: return sweep_dvnd_launch<128, 16>(tiles, ntiles, jobs, local, s);
+    case 8: return sweep_dvnd_launch<32, 32>(tiles, ntiles, jobs, local, s);
+    case 9: return sweep_dvnd_launch<64, 32>(tiles, ntiles, jobs, local, s);
+    // Two diagonals per thread from the term tables; with tile-local terms
+    // the same tiles run one diagonal per thread.
+    case 10: return local ? sweep_dvnd_launch<64, 8>(tiles, ntiles, jobs, true, s)
+                          : sweep_dvnd2_launch<64, 8>(tiles, ntiles, jobs, s);
+    case 11: return local ? sweep_dvnd_launch<64, 16>(tiles, ntiles, jobs, true, s)
+                          : sweep_dvnd2_launch<64, 16>(tiles, ntiles, jobs, s);
+    case 12: return local ? sweep_dvnd_launch<64, 32>(tiles, ntiles, jobs, true, s)
+                          : sweep_dvnd2_launch<64, 32>(tiles, ntiles, jobs, s);
+    case 13: return local ? sweep_dvnd_launch<128, 16>(tiles, ntiles, jobs, true, s)
+                          : sweep_dvnd2_launch<128, 16>(tiles, ntiles, jobs, s);
     default: return cudaErrorInvalidValue;
   }
 }

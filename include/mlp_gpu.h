@@ -127,6 +127,10 @@ MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t iterations);
  * evaluate all five neighbourhoods), 0 the general fused sweep.  Results are
  * identical; the switch exists for measurement and testing. */
 MLP_API int mlp_solver_set_sweep_kernel(mlp_solver_t s, int32_t variant);
+/* Merge kernel of the solver's iterations (as mlp_batch_set_merge_mode; the
+ * default for one search is the six-CTA cluster).  Every mode gives the same
+ * results. */
+MLP_API int mlp_solver_set_merge_mode(mlp_solver_t s, int32_t mode);
 /* Candidate mode of every later pass / DVND of this solver.  0 (default): one
  * candidate per reference block (the ODC kernels).  1: TOTAL multi-improvement
  * (the reference's isTotal kernels, source/mlkernel.h:150-163,

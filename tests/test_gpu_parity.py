@@ -136,6 +136,25 @@ def test_dvnd_both_sweep_kernels_every_shape(mlpgpu_mod, kernel, n, seed, shape)
         (ost["cost"], ost["iterations"], ost["moves"], ost["evals"])
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("n,seed,wide", [(5, 41, False), (9, 42, True), (60, 43, False), (333, 44, True),
+                                         (1000, 45, False)])
+def test_dvnd_every_merge_kernel(mlpgpu_mod, mode, n, seed, wide):
+    """One search's DVND through the six-CTA cluster merge (1) and the one-CTA
+    merge (2) equals the oracle's."""
+    x, y = oracle.uniform_instance(n, seed)
+    D = oracle.dist(x, y, True)
+    t = oracle.random_perm_tour(n, seed)
+    s = mlpgpu_mod.Solver(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True), wide=wide)
+    s.set_merge_mode(mode)
+    s.set_tour(t)
+    st = s.dvnd()
+    ot, ost = oracle.dvnd(t, D, wide)
+    assert np.array_equal(s.tour(), ot)
+    assert (st["cost"], st["iterations"], st["moves"], st["evals"]) == \
+        (ost["cost"], ost["iterations"], ost["moves"], ost["evals"])
+
+
 def test_dvnd_subset_masks_and_iteration_cap(mlpgpu_mod):
     n = 250
     x, y = oracle.uniform_instance(n, 31)

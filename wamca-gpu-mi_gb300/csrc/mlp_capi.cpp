@@ -225,6 +225,11 @@ MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t u) {
   return s->set->set_unroll(u);
 }
 
+MLP_API int mlp_solver_set_merge_mode(mlp_solver_t s, int32_t mode) {
+  if (!s) return arg_error("null solver");
+  return s->set->set_merge_mode(mode);
+}
+
 MLP_API int mlp_solver_set_sweep_kernel(mlp_solver_t s, int32_t variant) {
   if (!s) return arg_error("null solver");
   return s->set->set_sweep_kernel(variant);

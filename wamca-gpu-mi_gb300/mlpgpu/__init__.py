@@ -101,6 +101,7 @@ def lib() -> C.CDLL:
         "mlp_solver_set_tile_shape": (C.c_int, [vp, i32]),
         "mlp_solver_set_unroll": (C.c_int, [vp, i32]),
         "mlp_solver_set_sweep_kernel": (C.c_int, [vp, i32]),
+        "mlp_solver_set_merge_mode": (C.c_int, [vp, i32]),
         "mlp_solver_set_total": (C.c_int, [vp, i32]),
         "mlp_solver_eval_oropt": (C.c_int, [vp, i32, vp, vp, vp]),
         "mlp_solver_pass_oropt": (C.c_int, [vp, i32, i32, vp, vp, vp, P(i32), P(i64)]),
@@ -308,6 +309,10 @@ class Solver:
         """DVND sweep kernel: 1 (default) row/column term tables, 0 the
         general fused sweep; identical results."""
         _check(lib().mlp_solver_set_sweep_kernel(self._h, variant))
+
+    def set_merge_mode(self, mode: int) -> None:
+        """0 automatic, 1 six-CTA cluster, 2 one CTA; identical results."""
+        _check(lib().mlp_solver_set_merge_mode(self._h, mode))
 
     def set_total(self, on: bool = True) -> None:
         """TOTAL multi-improvement (MLKernel isTotal): every evaluated move is a

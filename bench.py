@@ -755,9 +755,18 @@ def bench_grasp(args, mlpgpu, workloads):
         t0 = time.perf_counter()
         p.random_tours(seeds[q:q + 1], 0.5)
         one.append(time.perf_counter() - t0)
+    # The reference's own tie order (its std::sort restated on the device).
+    t0 = time.perf_counter()
+    rtours = p.random_tours(seeds, 0.5, ties=1)
+    t_ref = time.perf_counter() - t0
+    for q in range(4):
+        assert np.array_equal(rtours[q], oracle.random_tour(D, int(seeds[q]), 0.5)), "constructor mismatch"
     return {"workload": f"{count} starts of MLSolution::random(alpha=0.5) for the n={n} instance, one call "
                         "(seeds from the host, tours copied back)",
             "seconds": t, "starts_per_s": count / t, "one_start_ms": statistics.median(one) * 1e3,
+            "reference_ties": {"seconds": t_ref, "starts_per_s": count / t_ref,
+                               "note": "ties as the reference's std::sort leaves them (the sort restated per "
+                                       "step on one lane per start); bit-exact with MLSolution::random"},
             "cpu_oracle_ms_per_start": {"canonical_ties": (c1 - c0) / k * 1e3, "std_sort_ties": (c2 - c1) / k * 1e3,
                                         "sample": f"{k} starts each, 1 thread"}}
 

@@ -104,6 +104,13 @@ MLP_API int mlp_problem_info(mlp_problem_t p, int32_t* n, int32_t* size, int32_t
  * `tours` (count x size entries, host memory). */
 MLP_API int mlp_problem_random_tours(mlp_problem_t p, int32_t count, const uint32_t* seeds, float alpha,
                                      int32_t* tours);
+/* The same with the tie order chosen: ties = 0 as above (client id, one warp
+ * per start, a rank selection per step); ties = 1 the reference's own order,
+ * equal to MLSolution::random built with GCC's libstdc++: the persistent
+ * candidate array is re-sorted each step by a restatement of that library's
+ * std::sort (one warp per start, the sort on one lane; slower, for parity). */
+MLP_API int mlp_problem_random_tours_ties(mlp_problem_t p, int32_t count, const uint32_t* seeds, float alpha,
+                                          int32_t ties, int32_t* tours);
 /* Copies the n x n distance matrix to host memory. */
 MLP_API int mlp_problem_get_dist(mlp_problem_t p, int32_t* dist);
 MLP_API void mlp_problem_destroy(mlp_problem_t p);
@@ -154,6 +161,9 @@ MLP_API int mlp_solver_set_tour_device(mlp_solver_t s, const int32_t* tour_dev, 
  * reference's std::sort leaves their order to the library).  alpha in [0, 1].
  * Rebuilds the ADS. */
 MLP_API int mlp_solver_random_tour(mlp_solver_t s, uint32_t seed, float alpha);
+/* As mlp_solver_random_tour with the tie order chosen (see
+ * mlp_problem_random_tours_ties; ties = 1 reproduces MLSolution::random). */
+MLP_API int mlp_solver_random_tour_ties(mlp_solver_t s, uint32_t seed, float alpha, int32_t ties);
 MLP_API int mlp_solver_get_tour(mlp_solver_t s, int32_t* tour, int32_t len);
 /* Checkpoint / resume in the text format of MLSolution::save / load
  * (source/mlsolution.cpp:685-751): tour length, cost, the tour.  Loading
@@ -278,6 +288,9 @@ MLP_API int mlp_batch_set_sweep_kernel(mlp_batch_t b, int32_t variant);
 /* Adds a search whose start is MLSolution::random(seed, alpha), built on the
  * device when the batch is (re)started (as mlp_solver_random_tour). */
 MLP_API int mlp_batch_add_random(mlp_batch_t b, mlp_problem_t p, uint32_t seed, float alpha, int32_t* job);
+/* As mlp_batch_add_random with the tie order chosen (see mlp_problem_random_tours_ties). */
+MLP_API int mlp_batch_add_random_ties(mlp_batch_t b, mlp_problem_t p, uint32_t seed, float alpha, int32_t ties,
+                                      int32_t* job);
 /* Candidate mode of the batch's searches (as mlp_solver_set_total). */
 MLP_API int mlp_batch_set_total(mlp_batch_t b, int32_t on);
 /* Iterations between the host's convergence checks (default 16); after each

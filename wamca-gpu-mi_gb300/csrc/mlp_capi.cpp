@@ -250,22 +250,28 @@ MLP_API int mlp_solver_set_tour(mlp_solver_t s, const int32_t* tour, int32_t len
   return s->set->prepare(true);
 }
 
-MLP_API int mlp_solver_random_tour(mlp_solver_t s, uint32_t seed, float alpha) {
+MLP_API int mlp_solver_random_tour_ties(mlp_solver_t s, uint32_t seed, float alpha, int32_t ties) {
   MLP_RANGE("mlp_solver_random_tour");
   if (!s) return arg_error("null solver");
   MLP_TRY(check_alpha(alpha));
-  const std::vector<GraspTask> task{GraspTask{s->prob->dD, s->job->dev.tour, s->prob->n, seed, alpha, 0}};
+  if (ties < 0 || ties > 1) return arg_error("ties must be 0 (client id) or 1 (the reference's sort)");
+  const std::vector<GraspTask> task{GraspTask{s->prob->dD, s->job->dev.tour, s->prob->n, seed, alpha, ties, 0}};
   MLP_TRY(build_random_tours(task, s->set->stream()));
   return s->set->prepare(true);
 }
 
-MLP_API int mlp_problem_random_tours(mlp_problem_t h, int32_t count, const uint32_t* seeds, float alpha,
-                                     int32_t* tours) {
+MLP_API int mlp_solver_random_tour(mlp_solver_t s, uint32_t seed, float alpha) {
+  return mlp_solver_random_tour_ties(s, seed, alpha, 0);
+}
+
+MLP_API int mlp_problem_random_tours_ties(mlp_problem_t h, int32_t count, const uint32_t* seeds, float alpha,
+                                          int32_t ties, int32_t* tours) {
   MLP_RANGE("mlp_problem_random_tours");
   Problem* p = reinterpret_cast<Problem*>(h);
   if (!p) return arg_error("null problem");
   if (count < 0 || (count > 0 && (!seeds || !tours))) return arg_error("count must be >= 0 with seeds and tours");
   MLP_TRY(check_alpha(alpha));
+  if (ties < 0 || ties > 1) return arg_error("ties must be 0 (client id) or 1 (the reference's sort)");
   if (count == 0) return kOk;
   const size_t sz = (size_t)p->size;
   struct Res {
@@ -282,12 +288,18 @@ MLP_API int mlp_problem_random_tours(mlp_problem_t h, int32_t count, const uint3
   MLP_CUDA(cudaStreamCreateWithFlags(&r.st, cudaStreamNonBlocking), "stream");
   MLP_CUDA(cudaMallocAsync(&r.d, sizeof(int32_t) * sz * (size_t)count, r.st), "cudaMallocAsync(tours)");
   std::vector<GraspTask> tasks;
-  for (int32_t q = 0; q < count; q++) tasks.push_back(GraspTask{p->dD, r.d + q * sz, p->n, seeds[q], alpha, 0});
+  for (int32_t q = 0; q < count; q++)
+    tasks.push_back(GraspTask{p->dD, r.d + q * sz, p->n, seeds[q], alpha, ties, 0});
   MLP_TRY(build_random_tours(tasks, r.st));
   MLP_CUDA(cudaMemcpyAsync(tours, r.d, sizeof(int32_t) * sz * (size_t)count, cudaMemcpyDeviceToHost, r.st),
            "copy tours");
   MLP_CUDA(cudaStreamSynchronize(r.st), "copy tours");
   return kOk;
+}
+
+MLP_API int mlp_problem_random_tours(mlp_problem_t h, int32_t count, const uint32_t* seeds, float alpha,
+                                     int32_t* tours) {
+  return mlp_problem_random_tours_ties(h, count, seeds, alpha, 0, tours);
 }
 
 MLP_API int mlp_solver_set_tour_device(mlp_solver_t s, const int32_t* tour, int32_t len) {
@@ -760,24 +772,34 @@ MLP_API int mlp_batch_add(mlp_batch_t b, mlp_problem_t h, const int32_t* tour, i
   MLP_TRY(job_create(p, b->wide, 0, &j));
   b->jobs.emplace_back(j);
   b->tours.emplace_back(tour, tour + len);
-  b->random_start.emplace_back(0u, 0.0f);
+  b->random_start.emplace_back();
+  b->set.reset();
+  if (job) *job = (int32_t)b->jobs.size() - 1;
+  return kOk;
+}
+
+MLP_API int mlp_batch_add_random_ties(mlp_batch_t b, mlp_problem_t h, uint32_t seed, float alpha, int32_t ties,
+                                      int32_t* job) {
+  Problem* p = reinterpret_cast<Problem*>(h);
+  if (!b || !p) return arg_error("null argument");
+  MLP_TRY(check_alpha(alpha));
+  if (ties < 0 || ties > 1) return arg_error("ties must be 0 (client id) or 1 (the reference's sort)");
+  Job* j = nullptr;
+  MLP_TRY(job_create(p, b->wide, 0, &j));
+  b->jobs.emplace_back(j);
+  b->tours.emplace_back();
+  mlp_batch::RandomStart rs;
+  rs.seed = seed;
+  rs.alpha = alpha;
+  rs.ties = ties;
+  b->random_start.push_back(rs);
   b->set.reset();
   if (job) *job = (int32_t)b->jobs.size() - 1;
   return kOk;
 }
 
 MLP_API int mlp_batch_add_random(mlp_batch_t b, mlp_problem_t h, uint32_t seed, float alpha, int32_t* job) {
-  Problem* p = reinterpret_cast<Problem*>(h);
-  if (!b || !p) return arg_error("null argument");
-  MLP_TRY(check_alpha(alpha));
-  Job* j = nullptr;
-  MLP_TRY(job_create(p, b->wide, 0, &j));
-  b->jobs.emplace_back(j);
-  b->tours.emplace_back();
-  b->random_start.emplace_back(seed, alpha);
-  b->set.reset();
-  if (job) *job = (int32_t)b->jobs.size() - 1;
-  return kOk;
+  return mlp_batch_add_random_ties(b, h, seed, alpha, 0, job);
 }
 
 static int batch_upload(mlp_batch* b) {
@@ -785,8 +807,8 @@ static int batch_upload(mlp_batch* b) {
   for (size_t q = 0; q < b->jobs.size(); q++) {
     Job* j = b->jobs[q].get();
     if (b->tours[q].empty()) {
-      tasks.push_back(GraspTask{j->prob->dD, j->dev.tour, j->prob->n, b->random_start[q].first,
-                                b->random_start[q].second, 0});
+      const mlp_batch::RandomStart& rs = b->random_start[q];
+      tasks.push_back(GraspTask{j->prob->dD, j->dev.tour, j->prob->n, rs.seed, rs.alpha, rs.ties, 0});
       continue;
     }
     MLP_CUDA(cudaMemcpyAsync(j->dev.tour, b->tours[q].data(), sizeof(int32_t) * b->tours[q].size(),

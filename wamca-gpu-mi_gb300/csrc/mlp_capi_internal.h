@@ -43,7 +43,12 @@ struct mlp_batch {
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<mlp::Job>> jobs;
   std::vector<std::vector<int32_t>> tours;  // empty: the start is built on the device
-  std::vector<std::pair<uint32_t, float>> random_start;  // (seed, alpha) of those
+  struct RandomStart {
+    uint32_t seed = 0;
+    float alpha = 0;
+    int32_t ties = 0;
+  };
+  std::vector<RandomStart> random_start;  // seed, alpha and tie order of those
   std::unique_ptr<mlp::JobSet> set;
   ~mlp_batch();
 };

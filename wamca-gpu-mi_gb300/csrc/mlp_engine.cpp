@@ -488,23 +488,45 @@ int build_random_tours(const std::vector<GraspTask>& tasks, cudaStream_t stream)
     cudaStream_t st;
     GraspTask* tasks = nullptr;
     int* err = nullptr;
+    uint32_t* scratch = nullptr;
     ~Buffers() {
       if (tasks) cudaFreeAsync(tasks, st);
       if (err) cudaFreeAsync(err, st);
+      if (scratch) cudaFreeAsync(scratch, st);
     }
   } b{stream};
-  for (const GraspTask& t : tasks)
-    if (t.n < 1 || t.n > kMaxSize - 1 || !t.D || !t.tour) {
-      set_error("constructor task out of range");
-      return kErrArg;
+  // Canonical-tie tasks first, then the reference-tie ones (one launch each);
+  // the latter above kGraspRefSmemN nodes get 2n words of scratch.
+  std::vector<GraspTask> order;
+  int64_t words = 0;
+  for (int pass = 0; pass < 2; pass++)
+    for (GraspTask t : tasks) {
+      if (t.n < 1 || t.n > kMaxSize - 1 || !t.D || !t.tour || t.ties < 0 || t.ties > 1) {
+        set_error("constructor task out of range");
+        return kErrArg;
+      }
+      if (t.ties != pass) continue;
+      t.scratch = 0;
+      if (t.ties && t.n > kGraspRefSmemN) {
+        t.scratch = words;
+        words += 2 * (int64_t)t.n;
+      }
+      order.push_back(t);
     }
-  MLP_CUDA(cudaMallocAsync(&b.tasks, sizeof(GraspTask) * tasks.size(), stream), "cudaMallocAsync(constructor tasks)");
+  int ncanon = 0;
+  while (ncanon < (int)order.size() && order[ncanon].ties == 0) ncanon++;
+  MLP_CUDA(cudaMallocAsync(&b.tasks, sizeof(GraspTask) * order.size(), stream), "cudaMallocAsync(constructor tasks)");
   MLP_CUDA(cudaMallocAsync(&b.err, sizeof(int), stream), "cudaMallocAsync(constructor flag)");
-  MLP_CUDA(cudaMemcpyAsync(b.tasks, tasks.data(), sizeof(GraspTask) * tasks.size(), cudaMemcpyHostToDevice,
+  if (words > 0)
+    MLP_CUDA(cudaMallocAsync(&b.scratch, sizeof(uint32_t) * (size_t)words, stream),
+             "cudaMallocAsync(constructor scratch)");
+  MLP_CUDA(cudaMemcpyAsync(b.tasks, order.data(), sizeof(GraspTask) * order.size(), cudaMemcpyHostToDevice,
                            stream),
            "copy constructor tasks");
   MLP_CUDA(cudaMemsetAsync(b.err, 0, sizeof(int), stream), "memset(constructor flag)");
-  MLP_CUDA(launch_grasp(b.tasks, (int)tasks.size(), b.err, stream), "constructor kernel");
+  MLP_CUDA(launch_grasp(b.tasks, ncanon, 0, nullptr, b.err, stream), "constructor kernel");
+  MLP_CUDA(launch_grasp(b.tasks + ncanon, (int)order.size() - ncanon, 1, b.scratch, b.err, stream),
+           "constructor kernel");
   int herr = 0;
   MLP_CUDA(cudaMemcpyAsync(&herr, b.err, sizeof(int), cudaMemcpyDeviceToHost, stream), "read constructor flag");
   MLP_CUDA(cudaStreamSynchronize(stream), "constructor");

@@ -22,6 +22,7 @@
 
 #include "mlp_common.cuh"
 #include "mlp_kernels.cuh"
+#include "mlp_refsort.cuh"
 
 namespace mlp {
 
@@ -225,16 +226,91 @@ __global__ void __launch_bounds__(32 * kGraspWarps)
   }
 }
 
+// MLSolution::random with the reference's own order of equal distances: the
+// candidate array persists across steps exactly as clCands does
+// (mlsolution.cpp:766-855) -- the clients 1..n-1 in id order at first; each
+// step draws rclIndex (before sorting, as the reference), sorts the array by
+// distance to the client added last with the reference's sort (ascending for
+// alpha >= 0.5, descending otherwise, then rclIndex = count - rclIndex - 1),
+// takes that entry and closes the gap by shifting the tail left.  One warp
+// per start: the lanes gather the step's distances, lane 0 draws, sorts and
+// shifts.  Up to kGraspRefSmemN nodes the arrays live in shared memory, else
+// in the task's 2n words of the scratch buffer.
+constexpr size_t kGraspRefSmem = (size_t)kMtN * 4 + (size_t)kGraspRefSmemN * 8;
+
+__global__ void __launch_bounds__(32)
+    k_grasp_ref(const GraspTask* __restrict__ tasks, uint32_t* __restrict__ scratch) {
+  extern __shared__ __align__(16) uint8_t gsm[];
+  const int lane = threadIdx.x;
+  const GraspTask task = tasks[blockIdx.x];
+  const int32_t* __restrict__ D = task.D;
+  const int n = task.n;
+  const float alpha = task.alpha;
+  const bool desc = alpha < 0.5f;
+  int32_t* t = task.tour;
+  uint32_t* st = (uint32_t*)gsm;
+  uint32_t* keys;
+  int32_t* ids;
+  if (n <= kGraspRefSmemN) {
+    keys = st + kMtN;
+    ids = (int32_t*)(keys + kGraspRefSmemN);
+  } else {
+    keys = scratch + task.scratch;
+    ids = (int32_t*)(keys + n);
+  }
+  int pos = kMtN;
+  if (lane == 0) {
+    mt_seed(st, task.seed);
+    t[0] = 0;
+    t[n] = 0;
+  }
+  for (int q = lane; q < n - 1; q += 32) ids[q] = q + 1;
+  __syncwarp();
+  int last = 0;
+  for (int len = 1; len < n; len++) {
+    const int cnt = n - len;
+    uint32_t idx = 0;
+    if (cnt > 1) {
+      if (lane == 0) {
+        const uint32_t rcl = (uint32_t)ceilf(__fmul_rn(alpha, (float)cnt));
+        idx = rcl > 0 ? mt_rand_max(st, &pos, rcl - 1) : 0u;
+      }
+      const int32_t* __restrict__ row = D + (size_t)last * n;
+      for (int x = lane; x < cnt; x += 32) keys[x] = (uint32_t)row[ids[x]];
+      __syncwarp();
+      if (lane == 0) {
+        RefSort(keys, ids, desc).sort(cnt);
+        if (desc) idx = (uint32_t)cnt - idx - 1u;
+      }
+    }
+    int32_t cur = 0;
+    if (lane == 0) {
+      if (idx >= (uint32_t)cnt) idx = cnt - 1;  // alpha <= 1 (checked by the host) keeps idx < cnt
+      cur = ids[idx];
+      t[len] = cur;
+      for (int q = (int)idx; q + 1 < cnt; q++) ids[q] = ids[q + 1];
+    }
+    last = __shfl_sync(kFull, cur, 0);
+    __syncwarp();
+  }
+}
+
 }  // namespace
 
 cudaError_t configure_grasp() {
-  return cudaFuncSetAttribute(k_grasp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GraspSmem::total);
+  cudaError_t e = cudaFuncSetAttribute(k_grasp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GraspSmem::total);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_grasp_ref, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGraspRefSmem);
 }
 
-cudaError_t launch_grasp(const GraspTask* tasks, int count, int* err, cudaStream_t s) {
+cudaError_t launch_grasp(const GraspTask* tasks, int count, int ties, uint32_t* scratch, int* err, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   const cudaError_t e = configure_grasp();
   if (e != cudaSuccess) return e;
+  if (ties) {
+    k_grasp_ref<<<count, 32, kGraspRefSmem, s>>>(tasks, scratch);
+    return cudaGetLastError();
+  }
   const int grid = (count + kGraspWarps - 1) / kGraspWarps;
   k_grasp<<<grid, 32 * kGraspWarps, GraspSmem::total, s>>>(tasks, count, err);
   return cudaGetLastError();

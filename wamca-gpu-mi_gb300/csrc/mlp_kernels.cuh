@@ -83,8 +83,11 @@ cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool u
 // Opt the TOTAL greedy into its dynamic shared memory (configure_merge calls it).
 cudaError_t configure_total();
 // MLSolution::random on the device (mlp_grasp.cu): one start per task, its
-// n + 1 entries written to `tour` (device), MTRandom seeded with `seed`,
-// equal distances ordered by client id; alpha in [0, 1].  *err (device)
+// n + 1 entries written to `tour` (device), MTRandom seeded with `seed`;
+// alpha in [0, 1].  ties = 0: equal distances ordered by client id (one warp
+// per start, a rank selection per step); ties = 1: the reference's own order,
+// its std::sort of the persistent candidate array restated step for step
+// (mlp_refsort.cuh; one warp per start, the sort on one lane).  *err (device)
 // counts starts that failed an internal check (none expected).
 struct GraspTask {
   const int32_t* D;  // n x n distances
@@ -92,10 +95,13 @@ struct GraspTask {
   int32_t n;
   uint32_t seed;
   float alpha;
-  int32_t pad;
+  int32_t ties;
+  int64_t scratch;   // ties = 1 and n > kGraspRefSmemN: word offset of 2n words in the scratch buffer
 };
+constexpr int kGraspRefSmemN = 2048;  // ties = 1: up to this n the candidate arrays stay in shared memory
 cudaError_t configure_grasp();
-cudaError_t launch_grasp(const GraspTask* tasks, int count, int* err, cudaStream_t s);
+// tasks holds `count` tasks of one ties mode; scratch: see GraspTask::scratch.
+cudaError_t launch_grasp(const GraspTask* tasks, int count, int ties, uint32_t* scratch, int* err, cudaStream_t s);
 // Or-opt-k for any k in [1, kMaxOroptK] on one job: the per-block candidates
 // (oropt_blocks(k, size) keys, (delta, ctx) as the sweep's) and the pass over
 // them (greedy, apply; rebuild the ADS afterwards with launch_prepare).

@@ -139,8 +139,11 @@ def lib() -> C.CDLL:
         "mlp_batch_set_check_interval": (C.c_int, [vp, i32]),
         "mlp_batch_add": (C.c_int, [vp, vp, vp, i32, P(i32)]),
         "mlp_batch_add_random": (C.c_int, [vp, vp, C.c_uint32, C.c_float, P(i32)]),
+        "mlp_batch_add_random_ties": (C.c_int, [vp, vp, C.c_uint32, C.c_float, i32, P(i32)]),
         "mlp_solver_random_tour": (C.c_int, [vp, C.c_uint32, C.c_float]),
+        "mlp_solver_random_tour_ties": (C.c_int, [vp, C.c_uint32, C.c_float, i32]),
         "mlp_problem_random_tours": (C.c_int, [vp, i32, vp, C.c_float, vp]),
+        "mlp_problem_random_tours_ties": (C.c_int, [vp, i32, vp, C.c_float, i32, vp]),
         "mlp_batch_run": (C.c_int, [vp, i32, i32]),
         "mlp_batch_reset": (C.c_int, [vp]),
         "mlp_batch_result": (C.c_int, [vp, i32, vp, i32, P(DvndStats)]),
@@ -255,12 +258,14 @@ class Problem:
         _check(lib().mlp_problem_get_dist(self._h, _ptr(D)))
         return D
 
-    def random_tours(self, seeds: Sequence[int], alpha: float = 0.5) -> np.ndarray:
+    def random_tours(self, seeds: Sequence[int], alpha: float = 0.5, ties: int = 0) -> np.ndarray:
         """Starts of MLSolution::random(seed, alpha) built on the device, one row
-        per seed (equal distances taken in client-id order)."""
+        per seed; equal distances in client-id order (ties=0) or in the
+        reference's own std::sort order (ties=1)."""
         sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint32))
         out = np.zeros((len(sd), self.n + 1), np.int32)
-        _check(lib().mlp_problem_random_tours(self._h, len(sd), _ptr(sd), C.c_float(alpha), _ptr(out)))
+        _check(lib().mlp_problem_random_tours_ties(self._h, len(sd), _ptr(sd), C.c_float(alpha), int(ties),
+                                                   _ptr(out)))
         return out
 
     def close(self) -> None:
@@ -323,9 +328,10 @@ class Solver:
         t = _i32(tour)
         _check(lib().mlp_solver_set_tour(self._h, _ptr(t), len(t)))
 
-    def random_tour(self, seed: int, alpha: float = 0.5) -> None:
-        """The tour becomes MLSolution::random(seed, alpha), built on the device."""
-        _check(lib().mlp_solver_random_tour(self._h, seed, C.c_float(alpha)))
+    def random_tour(self, seed: int, alpha: float = 0.5, ties: int = 0) -> None:
+        """The tour becomes MLSolution::random(seed, alpha), built on the device
+        (ties as in Problem.random_tours)."""
+        _check(lib().mlp_solver_random_tour_ties(self._h, seed, C.c_float(alpha), int(ties)))
 
     def set_tour_device(self, ptr: int) -> None:
         _check(lib().mlp_solver_set_tour_device(self._h, C.c_void_p(ptr), self.size))
@@ -497,10 +503,11 @@ class Batch:
         self._problems.append(problem)
         return j.value
 
-    def add_random(self, problem: Problem, seed: int, alpha: float = 0.5) -> int:
-        """Adds a search whose start MLSolution::random(seed, alpha) is built on the device."""
+    def add_random(self, problem: Problem, seed: int, alpha: float = 0.5, ties: int = 0) -> int:
+        """Adds a search whose start MLSolution::random(seed, alpha) is built on
+        the device (ties as in Problem.random_tours)."""
         j = C.c_int32()
-        _check(lib().mlp_batch_add_random(self._h, problem._h, seed, C.c_float(alpha), C.byref(j)))
+        _check(lib().mlp_batch_add_random_ties(self._h, problem._h, seed, C.c_float(alpha), int(ties), C.byref(j)))
         self.sizes.append(problem.n + 1)
         self._problems.append(problem)
         return j.value

@@ -22,8 +22,8 @@
  *   - Failures throw std::runtime_error with mlp_last_error().
  *   - MLSolution::random is the reference's constructor on the host (with
  *     std::sort, so equal distances are ordered by the same library as the
- *     reference's); randomDevice builds it on the GPU with equal distances
- *     in client-id order.
+ *     reference's); randomDevice builds it on the GPU, with equal distances
+ *     in client-id order or (ties = 1) in the reference's own order.
  */
 #ifndef MLP_GPU_HPP
 #define MLP_GPU_HPP
@@ -216,10 +216,12 @@ class MLSolution {
     if (problem.costTour) add(0);
     update();
   }
-  /* The same constructor on the GPU (equal distances in client-id order). */
-  void randomDevice(uint32_t seed, float alpha) {
+  /* The same constructor on the GPU: ties = 0 takes equal distances in
+   * client-id order (fast); ties = 1 in the reference's own std::sort order
+   * (the same start as random()). */
+  void randomDevice(uint32_t seed, float alpha, int32_t ties = 0) {
     std::vector<int32_t> t(size);
-    check(mlp_problem_random_tours(problem.handle(), 1, &seed, alpha, t.data()));
+    check(mlp_problem_random_tours_ties(problem.handle(), 1, &seed, alpha, ties, t.data()));
     for (uint32_t i = 0; i < size; i++) clients[i] = (uint16_t)t[i];
     clientCount = size;
     update();

@@ -86,6 +86,14 @@ int main(int argc, char** argv) {
     host.random(r2, 0.90f);
     dev.randomDevice(0, 0.90f);
     EXPECT(host.tour() == dev.tour() && host.cost == dev.cost);
+    // With the reference's tie order the device start equals the host one on
+    // K3's own draw too, where ties decide picks (494309).
+    MTRandom r3;
+    r3.seed(0);
+    MLSolution host3(problem), dev3(problem);
+    host3.random(r3, 0.50f);
+    dev3.randomDevice(0, 0.50f, 1);
+    EXPECT(host3.tour() == dev3.tour() && host3.cost == dev3.cost);
   } catch (const std::exception& e) {
     std::printf("exception: %s\n", e.what());
     return 1;

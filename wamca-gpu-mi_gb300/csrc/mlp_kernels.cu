@@ -154,11 +154,19 @@ __device__ __forceinline__ void write_terms(const JobDev* J, int p, int sz, cons
 // (source/mlsolution.cpp:216-228 and :454-458 for T = W).  With t_prev, the
 // tour that J->w and J->A currently describe, a position whose window
 // t[p-1 .. p+3] is unchanged keeps its w and A (no distance gathers); w_prev,
-// when given, is a copy of J->w to read those from.
+// when given, is a copy of J->w to read those from.  With src as well
+// (t[p] = t_prev[src[p]], the applied moves' position map) every weight and
+// skip distance whose two clients were already kt + 1 positions apart in the
+// old tour, in either order (D is symmetric), is taken from the old arrays:
+// inside a reversed or shifted segment nothing is gathered, only around its
+// ends.  Every value is read before any is written (two phases).
 // --------------------------------------------------------------------------
+constexpr int kPrepMaxPer = 4;  // positions per thread of the two-phase rebuild
+
 template <bool WIDE>
 __device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_override, int32_t* w_s,
-                                            const int32_t* t_prev = nullptr, const int32_t* w_prev = nullptr) {
+                                            const int32_t* t_prev = nullptr, const int32_t* w_prev = nullptr,
+                                            const int32_t* src = nullptr) {
   using C = typename Arith<WIDE>::C;
   __shared__ C smW[32], smQ[32], smC[32];
   const int sz = J->size, n = J->n, pad = sz + 8;
@@ -196,7 +204,57 @@ __device__ __forceinline__ void cta_prepare(const JobDev* J, const int32_t* t_ov
     return wp;
   };
   C sW = 0, sQ = 0, sC = 0;
-  if (chunk == 1) {  // one position per thread at most
+  if (src != nullptr && t_prev != nullptr && chunk <= kPrepMaxPer) {
+    // Phase 1: the new w and A of this thread's positions (p = tid + u nt).
+    int32_t nw[kPrepMaxPer], na[kPrepMaxPer][3];
+    bool keep[kPrepMaxPer];
+#pragma unroll
+    for (int u = 0; u < kPrepMaxPer; u++) {
+      const int p = threadIdx.x + u * nt;
+      keep[u] = true;
+      nw[u] = 0;
+      na[u][0] = na[u][1] = na[u][2] = 0;
+      if (u >= chunk || p >= sz || p == 0) continue;
+      const int qa = src[p - 1], qb = src[p];
+      if (qb == qa + 1) {
+        nw[u] = w_prev != nullptr ? w_prev[qb] : w[qb];
+      } else if (qa == qb + 1) {
+        nw[u] = w_prev != nullptr ? w_prev[qa] : w[qa];
+      } else {
+        nw[u] = D[(size_t)t[p - 1] * n + t[p]];
+      }
+      bool same = qa == p - 1 && qb == p;
+#pragma unroll
+      for (int k = 1; k <= 3; k++) {
+        if (p + k > sz - 1) continue;
+        const int qc = src[p + k];
+        same &= qc == p + k;
+        if (qc == qa + k + 1) na[u][k - 1] = A[(k - 1) * pad + qa + 1];
+        else if (qa == qc + k + 1) na[u][k - 1] = A[(k - 1) * pad + qc + 1];
+        else na[u][k - 1] = D[(size_t)t[p - 1] * n + t[p + k]];
+      }
+      keep[u] = same;  // window unchanged: the stored values stand
+    }
+    __syncthreads();
+    // Phase 2: stores (only where something changed) and the staged w.
+#pragma unroll
+    for (int u = 0; u < kPrepMaxPer; u++) {
+      const int p = threadIdx.x + u * nt;
+      if (u >= chunk || p >= sz) continue;
+      w_s[p] = nw[u];
+      if (keep[u]) continue;
+      w[p] = nw[u];
+#pragma unroll
+      for (int k = 0; k < 3; k++) A[k * pad + p] = na[u][k];
+    }
+    __syncthreads();
+    for (int p = p0; p < p1; p++) {
+      const C wp = (C)w_s[p];
+      sW += wp;
+      sQ += (C)p * wp;
+      sC += (C)(sz - p) * wp;
+    }
+  } else if (chunk == 1) {  // one position per thread at most
     if (p0 < p1) {
       const C wp = (C)gather(p0);
       sW = wp;
@@ -927,7 +985,7 @@ template <bool WIDE>
 __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, const uint64_t* key3, const uint64_t* shp3,
                              const uint32_t* ij3, volatile uint8_t* st3, uint32_t* bits, int32_t* owner,
                              int32_t* t_old, int32_t* t_new, uint32_t* bits_big = nullptr,
-                             const int32_t* w_old = nullptr, bool reset_keys = true) {
+                             const int32_t* w_old = nullptr, bool reset_keys = true, int bits_words = 0) {
   __shared__ uint32_t s_in[kBitMaxWs / 32], s_und[kBitMaxWs / 32];
   __shared__ int s_ns;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -935,6 +993,9 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
   int32_t* tour = J->tour;
   if (tid == 0) s_ns = 0;
   __syncthreads();
+  // The conflict-bit area (bits_words words, dead once stage 3 is decided)
+  // then holds the applied moves' position map for the ADS rebuild.
+  int32_t* const srcmap = bits_words >= sz ? reinterpret_cast<int32_t*>(bits) : nullptr;
   if (m3 > kBitMax) bits = m3 <= kBitMaxWs ? bits_big : nullptr;
   if (bits != nullptr) {
     // conflict rows: bit y of row x <=> y precedes x and !canMerge(y, x)
@@ -1043,10 +1104,11 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
   __syncthreads();
   for (int p = tid; p < sz; p += nt) {
     const int o = owner[p];
-    int32_t v = t_old[p];
-    if (o >= 0) v = t_old[move_source(id_of(key3[o]), (int)(ij3[o] & 0xffff), (int)(ij3[o] >> 16), p)];
+    const int q = o >= 0 ? move_source(id_of(key3[o]), (int)(ij3[o] & 0xffff), (int)(ij3[o] >> 16), p) : p;
+    const int32_t v = t_old[q];
     t_new[p] = v;
     tour[p] = v;
+    if (srcmap != nullptr) srcmap[p] = q;
   }
   const int ns = s_ns;
   // Applied moves in (delta, neighbourhood, block) order, for callers that
@@ -1074,7 +1136,7 @@ __device__ __forceinline__ void merge_finish(const JobDev* J, int sz, int m3, co
     else atomicExch(&stt[kStatConverged], 1ull);
   }
   __syncthreads();
-  cta_prepare<WIDE>(J, t_new, owner, t_old, w_old);  // the owner map is dead: w staging
+  cta_prepare<WIDE>(J, t_new, owner, t_old, w_old, srcmap);  // the owner map is dead: w staging
   if (reset_keys) cta_reset_keys(J);
   else if (J->tcount != nullptr && tid < kNumNb) J->tcount[tid] = 0;
 }
@@ -1240,7 +1302,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   }
   uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(use_smem ? &s_job : J, sz, s_m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits),
-                     (int32_t*)(ws + lay.o_owner), t_old, t_new, big, w_old, false);
+                     (int32_t*)(ws + lay.o_owner), t_old, t_new, big, w_old, false,
+                     (int)((lay.o_owner - lay.o_bits) / 4));
 }
 
 // --------------------------------------------------------------------------
@@ -1342,7 +1405,7 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
   __syncthreads();
   uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
-                     t_old, (int32_t*)(ws + lay.o_tnew), big, nullptr, false);
+                     t_old, (int32_t*)(ws + lay.o_tnew), big, nullptr, false, (int)((lay.o_owner - lay.o_bits) / 4));
 }
 
 // --------------------------------------------------------------------------
@@ -1521,7 +1584,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_total_finish(const JobDev* __
   __syncthreads();
   uint32_t* big = (!use_smem && lay.m3cap > kBitMax) ? (uint32_t*)(J->ws + ws_big_bits_offset(sz)) : nullptr;
   merge_finish<WIDE>(J, sz, m3, key3, shp3, ij3, st3, (uint32_t*)(ws + lay.o_bits), (int32_t*)(ws + lay.o_owner),
-                     t_old, (int32_t*)(ws + lay.o_tnew), big);
+                     t_old, (int32_t*)(ws + lay.o_tnew), big, nullptr, true, (int)((lay.o_owner - lay.o_bits) / 4));
 }
 
 // --------------------------------------------------------------------------

@@ -82,6 +82,28 @@ def test_total_batch_equals_alone(mlpgpu_mod):
         assert bst["cost"] == ost["cost"] and bst["moves"] == ost["moves"], q
 
 
+@pytest.mark.parametrize("count,wide", [(20, False), (70, True)])
+def test_total_batch_cluster_widths(mlpgpu_mod, count, wide):
+    # The greedy streams each list with a cluster of 8 CTAs for a few jobs and
+    # narrows the clusters as the batch grows (2 CTAs at 20 jobs, 1 at 70):
+    # every width gives the oracle's tours.
+    b = mlpgpu_mod.Batch(wide=wide)
+    b.set_total(True)
+    cases = []
+    for q in range(count):
+        n = 12 + (q * 37) % 90
+        x, y = (oracle.clustered_instance if q % 3 == 0 else oracle.uniform_instance)(n, 300 + q)
+        t = oracle.random_perm_tour(n, 300 + q)
+        b.add(mlpgpu_mod.Problem.from_coords(x, y, dist_round=True), t)
+        cases.append((x, y, t))
+    b.run()
+    for q, (x, y, t) in enumerate(cases):
+        ot, ost = oracle.dvnd_total(t, oracle.dist(x, y, True), wide)
+        bt, bst = b.result(q)
+        assert np.array_equal(bt, ot), q
+        assert bst["cost"] == ost["cost"] and bst["moves"] == ost["moves"], q
+
+
 @pytest.mark.parametrize("wide,nbs,iters", [(False, [0, 1], 2), (True, [1, 4], 1)])
 def test_total_large_size_global_workspace(mlpgpu_mod, wide, nbs, iters):
     # n = 2500: the finish runs from the job's global merge workspace (the

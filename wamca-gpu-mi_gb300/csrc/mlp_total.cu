@@ -9,22 +9,32 @@
 // mlkernel.cu:183-250): the greedy independent set in sorted order, here in
 // (delta, i, j) order.
 //
-// k_total_select: one CTA per (neighbourhood, job).  Its input is the list of
-// improving moves the collecting sweep appended (unordered, up to ~n^2/2
-// keys).  It never sorts the whole list: it repeatedly
+// k_total_select: one cluster of up to kTotCl CTAs per (neighbourhood, job).
+// Its input is the list of improving moves the collecting sweep appended
+// (unordered, up to ~n^2/2 keys), split into one slice per CTA.  It never
+// sorts the whole list: it repeatedly
 //   1. finds a threshold T with at most kTotBatch keys <= T (histogram of
 //      the keys' offsets from the smallest, refined into the lowest bin when
-//      that bin alone is too full),
-//   2. gathers those keys (the smallest of the list) and sorts them in shared
-//      memory,
-//   3. drops the ones that conflict with a move kept by earlier batches (a
-//      position bitmap of the kept moves), resolves the rest in order with a
-//      conflict bit matrix (lexicographically-first maximal independent set,
-//      as in the stage-3 merge) and adds the kept ones to the bitmap,
-//   4. filters the rest of the list against the bitmap, compacting in place.
-// Every move decided in step 3 only depends on moves with smaller keys, all
-// of them decided before, so the result is the sequential greedy's.  The kept
-// moves go to the job's TOTAL output region of the neighbourhood, in order.
+//      that bin alone is too full): every CTA histograms its slice and adds
+//      the cluster's histograms through distributed shared memory;
+//   2. gathers those keys (the smallest of the list) into the first CTA of
+//      the cluster; every CTA copies them and orders them by rank;
+//   3. resolves them in order with a conflict bit matrix (lexicographically
+//      first maximal independent set, as in the stage-3 merge; every CTA
+//      computes a share of the rows and stores them into all CTAs) and adds
+//      the kept ones to a position bitmap of the kept moves,
+//   4. filters the rest of its slice against the bitmap, compacting in
+//      place, and histograms the survivors for the next threshold.
+// Every CTA resolves each batch itself, so each holds the same bitmap; only
+// the first writes the kept moves.  No batch member conflicts with a move
+// kept by an earlier batch: step 4 removed those.  Every move decided in
+// step 3 only depends on moves with smaller keys, all of them decided before,
+// so the result is the sequential greedy's; the slicing changes only which
+// SM streams which keys (the list is a set).  The kept moves go to the job's
+// TOTAL output region of the neighbourhood, in order.  Cluster barriers order
+// every exchange through distributed shared memory.
+#include <cooperative_groups.h>
+
 #include <cstdint>
 
 #include "mlp_common.cuh"
@@ -33,6 +43,9 @@
 namespace mlp {
 
 namespace {
+
+namespace cg = cooperative_groups;
+constexpr int kTotCl = 8;  // most CTAs per neighbourhood list (portable cluster size)
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTotThreads = 1024;
@@ -75,14 +88,14 @@ __device__ __forceinline__ K kmax_value() {
 }
 
 struct TotalSmem {
-  static constexpr size_t bat = 0;                                         // K[kTotBatch]
-  static constexpr size_t hist = bat + (size_t)kTotBatch * 16;             // uint32[kTotBins]
-  static constexpr size_t cov = hist + (size_t)kTotBins * 4;               // uint32[kCovWords]
+  static constexpr size_t bat = 0;                                         // K[kTotBatch]: gathered batch
+  static constexpr size_t srt = bat + (size_t)kTotBatch * 16;              // K[kTotBatch]: the batch by rank
+  static constexpr size_t hist = srt + (size_t)kTotBatch * 16;             // uint32[2][kTotBins]
+  static constexpr size_t cov = hist + (size_t)2 * kTotBins * 4;           // uint32[kCovWords]
   static constexpr size_t pw = cov + (size_t)kCovWords * 4;                // int32[kCovWords]
   static constexpr size_t bits = pw + (size_t)kCovWords * 4;               // conflict rows
   static constexpr size_t ab = bits + (size_t)kTotBatch * kTotBatch / 8;   // uint32[kTotBatch]
-  static constexpr size_t idx = ab + (size_t)kTotBatch * 4;                // int32[kTotBatch]
-  static constexpr size_t st = idx + (size_t)kTotBatch * 4;                // uint8[kTotBatch]
+  static constexpr size_t st = ab + (size_t)kTotBatch * 4;                 // uint8[kTotBatch]
   static constexpr size_t total = st + kTotBatch;
 };
 
@@ -196,52 +209,111 @@ __device__ __forceinline__ bool conflict(int nb, uint32_t x, uint32_t y) {
   return xa <= yb && ya <= xb;
 }
 
+// The batch by rank: srt[r] = the key with r smaller keys (keys are
+// distinct: each encodes its move).  A warp ranks RK keys at a time against
+// the whole batch.
 template <bool WIDE>
-__global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __restrict__ jobs) {
+__device__ void rank_sort(const typename TK<WIDE>::K* bat, typename TK<WIDE>::K* srt, int nbat) {
   using K = typename TK<WIDE>::K;
-  extern __shared__ __align__(16) uint8_t tsm[];
-  __shared__ K s_red[64];
-  __shared__ int s_scan[32];
-  __shared__ int s_g, s_nbat;
-  __shared__ uint32_t s_in[kTotBatch / 32], s_und[kTotBatch / 32];
-  const int nb = blockIdx.x;
-  const JobDev* J = jobs + blockIdx.y;
-  {
-    const int64_t* stt = J->stats;
-    if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;
-  }
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-  const int sz = J->size;
-  if (!((J->nb_mask >> nb) & 1)) {
-    if (tid == 0) J->tkcount[nb] = 0;
-    return;
-  }
-  int m = J->tcount[nb];
-  if (m > total_list_cap(nb, sz)) {
-    if (tid == 0) {
-      J->stats[kStatError] = 4;
-      J->tkcount[nb] = 0;
+  constexpr int RK = WIDE ? 4 : 8;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int x0 = wid * RK; x0 < nbat; x0 += nw * RK) {
+    K kx[RK];
+    int c[RK];
+#pragma unroll
+    for (int k = 0; k < RK; k++) {
+      kx[k] = x0 + k < nbat ? bat[x0 + k] : kmax_value<K>();
+      c[k] = 0;
     }
-    return;
+    for (int y = lane; y < nbat; y += 32) {
+      const K ky = bat[y];
+#pragma unroll
+      for (int k = 0; k < RK; k++) c[k] += ky < kx[k] ? 1 : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < RK; k++) {
+      const int r = (int)__reduce_add_sync(kFull, (unsigned)c[k]);
+      if (lane == k && x0 + k < nbat) srt[r] = kx[k];
+    }
   }
-  K* list = (K*)J->tlist + total_list_off(nb, sz);
-  K* bat = (K*)(tsm + TotalSmem::bat);
-  uint32_t* hist = (uint32_t*)(tsm + TotalSmem::hist);
-  uint32_t* cov = (uint32_t*)(tsm + TotalSmem::cov);
-  int* pw = (int*)(tsm + TotalSmem::pw);
-  uint32_t* bits = (uint32_t*)(tsm + TotalSmem::bits);
-  uint32_t* mab = (uint32_t*)(tsm + TotalSmem::ab);
-  int* midx = (int*)(tsm + TotalSmem::idx);
-  volatile uint8_t* mst = (volatile uint8_t*)(tsm + TotalSmem::st);
-  const int nwords = (sz >> 5) + 2;  // bitmap words read for positions 0 .. sz
-  for (int w = tid; w < kCovWords; w += nt) {
-    cov[w] = 0;
-    pw[w] = 0;
+}
+
+// Rows rank, rank + ncl, ... of the batch's conflict matrix (bit y of row x:
+// y precedes x and the two conflict; only words 0 .. x/32 of row x exist),
+// stored into every CTA of the cluster.  W = words per row.
+__device__ void conflict_rows(cg::cluster_group& cluster, int nb, const uint32_t* mab, uint32_t* bits, int na, int W,
+                              int rank, int ncl) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int x = rank + ncl * wid; x < na; x += ncl * nw) {
+    const uint32_t fx = mab[x];
+    const int nwx = (x >> 5) + 1;
+    uint32_t word[kTotBatch / 32];
+#pragma unroll
+    for (int w = 0; w < kTotBatch / 32; w++) {
+      word[w] = 0u;
+      if (w < nwx) {
+        const int y = 32 * w + lane;  // mab is read for y < x < na only
+        word[w] = __ballot_sync(kFull, y < x && conflict(nb, mab[y], fx));
+      }
+    }
+    if (lane < ncl) {
+      uint32_t* dst = cluster.map_shared_rank(bits, lane) + x * W;
+#pragma unroll
+      for (int w = 0; w < kTotBatch / 32; w++)
+        if (w < nwx) dst[w] = word[w];
+    }
   }
-  const int kbase = region_off(nb, sz), kcap = region_cap(nb, sz);
-  int nk = 0;
-  K lo = kmax_value<K>(), hi = 0;
+}
+
+// Lexicographically first maximal independent set of the batch's conflict
+// matrix, by rounds: a member whose earlier conflicting members are all
+// decided out joins; one that conflicts with a member in leaves.
+__device__ void resolve_rows(const uint32_t* bits, volatile uint8_t* mst, uint32_t* s_in, uint32_t* s_und, int na,
+                             int W) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  for (int w = tid; w < W; w += nt) {
+    s_in[w] = 0;
+    const int rem = na - 32 * w;
+    s_und[w] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+  }
+  __syncthreads();
+  for (int r = 0; r <= na; r++) {
+    int any = 0;
+    for (int x = tid; x < na; x += nt) {
+      if (mst[x] != kUndec) continue;
+      uint32_t hin = 0, hund = 0;
+      for (int w = 0; w <= (x >> 5); w++) {
+        const uint32_t row = bits[x * W + w];
+        hin |= row & s_in[w];
+        hund |= row & s_und[w];
+      }
+      if (hin) mst[x] = kOut;
+      else if (!hund) mst[x] = kIn;
+      else any = 1;
+    }
+    __syncthreads();
+    for (int w = wid; w < W; w += nw) {
+      const int x = 32 * w + lane;
+      const uint8_t sx = x < na ? mst[x] : kNone;
+      const uint32_t bi = __ballot_sync(kFull, sx == kIn), bu = __ballot_sync(kFull, sx == kUndec);
+      if (lane == 0) {
+        s_in[w] = bi;
+        s_und[w] = bu;
+      }
+    }
+    if (!__syncthreads_or(any)) break;
+  }
+}
+
+// Histogram of the keys of list[0, m) in [lo, lo + range], bins of 2^sft.
+template <bool WIDE>
+__device__ void slice_hist(const typename TK<WIDE>::K* list, int m, uint32_t* hist, typename TK<WIDE>::K lo,
+                           typename TK<WIDE>::K range, int sft) {
+  using K = typename TK<WIDE>::K;
   constexpr int U = TK<WIDE>::U;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int q = tid; q < kTotBins; q += nt) hist[q] = 0;
+  __syncthreads();
   for (int x0 = 0; x0 < m; x0 += U * nt) {
     K kv[U];
 #pragma unroll
@@ -250,49 +322,148 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       kv[u] = x < m ? list[x] : kmax_value<K>();
     }
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int x = x0 + u * nt + tid;
-      if (x < m) {
-        lo = kv[u] < lo ? kv[u] : lo;
-        hi = kv[u] > hi ? kv[u] : hi;
+    for (int u = 0; u < U; u++) hist_add(hist, x0 + u * nt + tid < m ? bin_of(kv[u], lo, range, sft) : -1);
+  }
+}
+
+// Launched with clusters of 1 .. kTotCl CTAs along x (a cluster per
+// neighbourhood and job); blockIdx.y is the job.
+template <bool WIDE>
+__global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __restrict__ jobs) {
+  using K = typename TK<WIDE>::K;
+  extern __shared__ __align__(16) uint8_t tsm[];
+  __shared__ K s_red[64];
+  __shared__ K s_qlo[kTotCl], s_qhi[kTotCl];  // each CTA's bounds, stored by that CTA
+  __shared__ int s_qm[kTotCl];                // keys left in each CTA's slice, stored by that CTA
+  __shared__ int s_scan[32];
+  __shared__ int s_g, s_nbat, s_nb;
+  __shared__ uint32_t s_in[kTotBatch / 32], s_und[kTotBatch / 32];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank(), ncl = (int)cluster.num_blocks();
+  const bool first = rank == 0;
+  const int nb = blockIdx.x / ncl;
+  const JobDev* J = jobs + blockIdx.y;
+  // Exits before the first barrier are taken by the whole cluster (same job
+  // and neighbourhood).
+  {
+    const int64_t* stt = J->stats;
+    if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;
+  }
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+  const int sz = J->size;
+  if (!((J->nb_mask >> nb) & 1)) {
+    if (first && tid == 0) J->tkcount[nb] = 0;
+    return;
+  }
+  const int mall = J->tcount[nb];
+  if (mall > total_list_cap(nb, sz)) {
+    if (first && tid == 0) {
+      J->stats[kStatError] = 4;
+      J->tkcount[nb] = 0;
+    }
+    return;
+  }
+  // This CTA's slice of the list.
+  const int slice = (mall + ncl - 1) / ncl;
+  const int s0 = min(mall, rank * slice);
+  int m = min(mall, s0 + slice) - s0;
+  K* list = (K*)J->tlist + total_list_off(nb, sz) + s0;
+  K* bat = (K*)(tsm + TotalSmem::bat);
+  K* srt = (K*)(tsm + TotalSmem::srt);
+  uint32_t* hist = (uint32_t*)(tsm + TotalSmem::hist);
+  uint32_t* cov = (uint32_t*)(tsm + TotalSmem::cov);
+  int* pw = (int*)(tsm + TotalSmem::pw);
+  uint32_t* bits = (uint32_t*)(tsm + TotalSmem::bits);
+  uint32_t* mab = (uint32_t*)(tsm + TotalSmem::ab);
+  volatile uint8_t* mst = (volatile uint8_t*)(tsm + TotalSmem::st);
+  K* l_bat = cluster.map_shared_rank(bat, 0);
+  int* l_nbat = cluster.map_shared_rank(&s_nbat, 0);
+  const int nwords = (sz >> 5) + 2;  // bitmap words read for positions 0 .. sz
+  for (int w = tid; w < kCovWords; w += nt) {
+    cov[w] = 0;
+    pw[w] = 0;
+  }
+  if (tid == 0) s_nbat = 0;
+  const int kbase = region_off(nb, sz), kcap = region_cap(nb, sz);
+  int nk = 0;
+  constexpr int U = TK<WIDE>::U;
+  {
+    K lo = kmax_value<K>(), hi = 0;
+    for (int x0 = 0; x0 < m; x0 += U * nt) {
+      K kv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int x = x0 + u * nt + tid;
+        kv[u] = x < m ? list[x] : kmax_value<K>();
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int x = x0 + u * nt + tid;
+        if (x < m) {
+          lo = kv[u] < lo ? kv[u] : lo;
+          hi = kv[u] > hi ? kv[u] : hi;
+        }
       }
     }
+    block_minmax(lo, hi, s_red);
+    if (tid < ncl) {
+      *cluster.map_shared_rank(&s_qlo[rank], tid) = lo;
+      *cluster.map_shared_rank(&s_qhi[rank], tid) = hi;
+      *cluster.map_shared_rank(&s_qm[rank], tid) = m;
+    }
   }
-  block_minmax(lo, hi, s_red);
+  cluster.sync();
+  // Bounds of the whole list (a CTA with an empty slice reports none).
+  K lo = kmax_value<K>(), hi = 0;
+  int mtot = 0;
+  for (int q = 0; q < ncl; q++) {
+    if (s_qm[q] == 0) continue;
+    mtot += s_qm[q];
+    lo = s_qlo[q] < lo ? s_qlo[q] : lo;
+    hi = s_qhi[q] > hi ? s_qhi[q] : hi;
+  }
   K range = hi - lo;
   int sft = bin_shift(bitlen(range));
+  // Histograms alternate between two buffers: a CTA fills one while the
+  // others may still read the previous one.
+  int hb = 0;
+  if (mtot > kTotBatch) slice_hist<WIDE>(list, m, hist, lo, range, sft);
 
-  for (int round = 0; m > 0; round++) {
+  for (int round = 0;; round++) {
+    // Every slice count and first-level histogram is complete.
+    cluster.sync();
+    mtot = 0;
+    for (int q = 0; q < ncl; q++) mtot += s_qm[q];
+    if (mtot == 0) break;
     if (round > (1 << 24)) {  // unreachable: every round removes at least the smallest key
-      if (tid == 0) J->stats[kStatError] = 5;
+      if (first && tid == 0) J->stats[kStatError] = 5;
       break;
     }
     // ---- 1. threshold: at most kTotBatch keys <= T ----
-    // Every remaining key lies in [lo, hi]; histogram of [lo, lo + range] in
-    // bins of 2^sft.
     K T = hi;
-    if (m > kTotBatch) {
+    if (mtot > kTotBatch) {
       // Take the lowest bins that fit the budget; while less than half of
       // the batch is filled, refine into the first bin that did not fit.
       int budget = kTotBatch;
       bool have_t = false;
       for (int lvl = 0; lvl < 16; lvl++) {
-        for (int q = tid; q < kTotBins; q += nt) hist[q] = 0;
-        __syncthreads();
-        for (int x0 = 0; x0 < m; x0 += U * nt) {
-          K kv[U];
+        if (lvl > 0) {
+          hb ^= 1;
+          slice_hist<WIDE>(list, m, hist + hb * kTotBins, lo, range, sft);
+          cluster.sync();  // every CTA's histogram of this level is complete
+        }
+        // The list's histogram: every CTA adds the same histograms.
+        int h0 = 0, h1 = 0;
 #pragma unroll
-          for (int u = 0; u < U; u++) {
-            const int x = x0 + u * nt + tid;
-            kv[u] = x < m ? list[x] : kmax_value<K>();
+        for (int q = 0; q < kTotCl; q++) {
+          if (q < ncl) {
+            const uint2 v = *reinterpret_cast<const uint2*>(cluster.map_shared_rank(hist + hb * kTotBins, q) + 2 * tid);
+            h0 += (int)v.x;
+            h1 += (int)v.y;
           }
-#pragma unroll
-          for (int u = 0; u < U; u++)
-            hist_add(hist, x0 + u * nt + tid < m ? bin_of(kv[u], lo, range, sft) : -1);
         }
         if (tid == 0) s_g = -1;
         __syncthreads();
-        const int h0 = (int)hist[2 * tid], h1 = (int)hist[2 * tid + 1];
         int tot;
         const int e = block_scan_int(h0 + h1, s_scan, tot);
         // (last bin that fits) << 20 | (keys up to it): both grow together
@@ -315,9 +486,7 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       }
       if (!have_t) T = hi;  // unreachable: single-key bins always fit
     }
-    // ---- 2. gather the keys <= T and sort them ----
-    if (tid == 0) s_nbat = 0;
-    __syncthreads();
+    // ---- 2. the keys <= T go to the first CTA; every CTA copies them ----
     for (int x0 = 0; x0 < m; x0 += U * nt) {
       K kv[U];
 #pragma unroll
@@ -327,148 +496,90 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       }
 #pragma unroll
       for (int u = 0; u < U; u++) {
-        if (x0 + u * nt + tid < m && kv[u] <= T) {
-          const int q = atomicAdd(&s_nbat, 1);
-          if (q < kTotBatch) bat[q] = kv[u];
+        const bool g = x0 + u * nt + tid < m && kv[u] <= T;
+        const unsigned bal = __ballot_sync(kFull, g);
+        if (bal) {
+          const int src = __ffs(bal) - 1;
+          int base = 0;
+          if (lane == src) base = atomicAdd(l_nbat, __popc(bal));
+          base = __shfl_sync(kFull, base, src);
+          const int q = base + __popc(bal & ((1u << lane) - 1u));
+          if (g && q < kTotBatch) l_bat[q] = kv[u];
         }
       }
+    }
+    cluster.sync();  // the batch is complete
+    if (tid == 0) {
+      const int nbat = *l_nbat;
+      if (nbat > kTotBatch && first) J->stats[kStatError] = 5;  // unreachable by the threshold's construction
+      s_nb = nbat < kTotBatch ? nbat : kTotBatch;
     }
     __syncthreads();
-    int nbat = s_nbat;
-    if (nbat > kTotBatch) {  // unreachable by the threshold's construction
-      if (tid == 0) J->stats[kStatError] = 5;
-      nbat = kTotBatch;
-    }
-    int P = 1;
-    while (P < nbat) P <<= 1;
-    for (int q = nbat + tid; q < P; q += nt) bat[q] = kmax_value<K>();
+    const int na = s_nb;
+    const int W = (na + 31) >> 5;
+    if (!first)
+      for (int x = tid; x < na; x += nt) bat[x] = l_bat[x];
     __syncthreads();
-    for (int k2 = 2; k2 <= P; k2 <<= 1) {
-      for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
-        if (tid < P) {
-          const int o = tid ^ j2;
-          if (o > tid) {
-            const K a = bat[tid], b = bat[o];
-            const bool up = (tid & k2) == 0;
-            if ((a > b) == up) {
-              bat[tid] = b;
-              bat[o] = a;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    }
-    // ---- 3. resolve the batch in order ----
-    // Members not killed by earlier batches, compacted in key order.
-    bool alive = false;
-    uint32_t fab = 0;
-    if (tid < nbat) {
-      fab = footprint_of(nb, (uint32_t)bat[tid]);
-      alive = !killed(nb, fab, cov, pw);
-    }
-    int na;
-    const int pos = block_scan_int(alive ? 1 : 0, s_scan, na);
-    if (alive) {
-      mab[pos] = fab;
-      midx[pos] = tid;
-      mst[pos] = kUndec;
+    // ---- 3. resolve the batch in key order ----
+    rank_sort<WIDE>(bat, srt, na);
+    __syncthreads();
+    for (int x = tid; x < na; x += nt) {
+      mab[x] = footprint_of(nb, (uint32_t)srt[x]);
+      mst[x] = kUndec;
     }
     __syncthreads();
-    if (na > 0) {
-      const int W = (na + 31) >> 5;
-      // bit y of row x <=> y precedes x and the two conflict
-      for (int x = wid; x < na; x += nw) {
-        const uint32_t fx = mab[x];
-        for (int w0 = 0; w0 < W; w0 += 4) {
-          uint32_t word[4] = {0u, 0u, 0u, 0u};
-          if (32 * w0 < x) {  // words of members after x stay zero
-#pragma unroll
-            for (int d = 0; d < 4; d++) {
-              const int y = 32 * (w0 + d) + lane;  // mab is read for y < x < na only
-              word[d] = __ballot_sync(kFull, y < x && conflict(nb, mab[y], fx));
-            }
-          }
-          if (lane == 0) {
-#pragma unroll
-            for (int d = 0; d < 4; d++)
-              if (w0 + d < W) bits[x * W + w0 + d] = word[d];
-          }
-        }
+    conflict_rows(cluster, nb, mab, bits, na, W, rank, ncl);
+    cluster.sync();  // every CTA holds the whole conflict matrix
+    if (first && tid == 0) s_nbat = 0;  // every read of it precedes the barrier
+    resolve_rows(bits, mst, s_in, s_und, na, W);
+    // Kept members, in key order, to the output region.
+    const bool kin = tid < na && mst[tid] == kIn;
+    int nin;
+    const int krank = block_scan_int(kin ? 1 : 0, s_scan, nin);
+    if (first && kin) {
+      const int o = nk + krank;
+      if (o < kcap) {
+        const K k = srt[tid];
+        const uint32_t low = (uint32_t)k;
+        J->tkcost[kbase + o] = TK<WIDE>::delta(k);
+        J->tkij[kbase + o] = ((low >> 14) & 0x3fff) | ((low & 0x3fff) << 16);
       }
-      for (int w = tid; w < W; w += nt) {
-        s_in[w] = 0;
-        const int rem = na - 32 * w;
-        s_und[w] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
-      }
-      __syncthreads();
-      for (int r = 0; r <= na; r++) {
-        int any = 0;
-        for (int x = tid; x < na; x += nt) {
-          if (mst[x] != kUndec) continue;
-          uint32_t hin = 0, hund = 0;
-          for (int w = 0; w < W; w++) {
-            const uint32_t row = bits[x * W + w];
-            hin |= row & s_in[w];
-            hund |= row & s_und[w];
-          }
-          if (hin) mst[x] = kOut;
-          else if (!hund) mst[x] = kIn;
-          else any = 1;
-        }
-        __syncthreads();
-        for (int w = wid; w < W; w += nw) {
-          const int x = 32 * w + lane;
-          const uint8_t sx = x < na ? mst[x] : kNone;
-          const uint32_t bi = __ballot_sync(kFull, sx == kIn), bu = __ballot_sync(kFull, sx == kUndec);
-          if (lane == 0) {
-            s_in[w] = bi;
-            s_und[w] = bu;
-          }
-        }
-        if (!__syncthreads_or(any)) break;
-      }
-      // Kept members, in key order, to the output region.
-      const bool kin = tid < na && mst[tid] == kIn;
-      int nin;
-      const int rank = block_scan_int(kin ? 1 : 0, s_scan, nin);
+    }
+    nk += nin;
+    // Add the kept footprints to the bitmap.
+    if (nb == 0) {
       if (kin) {
-        const int o = nk + rank;
-        if (o < kcap) {
-          const K k = bat[midx[tid]];
-          const uint32_t low = (uint32_t)k;
-          J->tkcost[kbase + o] = TK<WIDE>::delta(k);
-          J->tkij[kbase + o] = ((low >> 14) & 0x3fff) | ((low & 0x3fff) << 16);
-        }
+        const int i = (int)(mab[tid] & 0xffff), j = (int)(mab[tid] >> 16);
+        atomicOr(&cov[i >> 5], 1u << (i & 31));
+        atomicOr(&cov[j >> 5], 1u << (j & 31));
       }
-      nk += nin;
-      // Add the kept footprints to the bitmap.
-      if (nb == 0) {
-        if (kin) {
-          const int i = (int)(mab[tid] & 0xffff), j = (int)(mab[tid] >> 16);
-          atomicOr(&cov[i >> 5], 1u << (i & 31));
-          atomicOr(&cov[j >> 5], 1u << (j & 31));
+    } else {
+      const int wid = tid >> 5, nw = nt >> 5;
+      for (int x = wid; x < na; x += nw) {
+        if (mst[x] != kIn) continue;
+        const int a = (int)(mab[x] & 0xffff), b = (int)(mab[x] >> 16);
+        for (int w = (a >> 5) + lane; w <= (b >> 5); w += 32) {
+          uint32_t msk = 0xffffffffu;
+          if (w == (a >> 5)) msk &= 0xffffffffu << (a & 31);
+          if (w == (b >> 5)) msk &= 0xffffffffu >> (31 - (b & 31));
+          atomicOr(&cov[w], msk);
         }
-      } else {
-        for (int x = wid; x < na; x += nw) {
-          if (mst[x] != kIn) continue;
-          const int a = (int)(mab[x] & 0xffff), b = (int)(mab[x] >> 16);
-          for (int w = (a >> 5) + lane; w <= (b >> 5); w += 32) {
-            uint32_t msk = 0xffffffffu;
-            if (w == (a >> 5)) msk &= 0xffffffffu << (a & 31);
-            if (w == (b >> 5)) msk &= 0xffffffffu >> (31 - (b & 31));
-            atomicOr(&cov[w], msk);
-          }
-        }
-        __syncthreads();
-        int tw;
-        const int cw = tid < nwords ? __popc(cov[tid]) : 0;
-        const int ew = block_scan_int(cw, s_scan, tw);
-        if (tid < nwords + 1) pw[tid] = ew;
       }
       __syncthreads();
+      int tw;
+      const int cw = tid < nwords ? __popc(cov[tid]) : 0;
+      const int ew = block_scan_int(cw, s_scan, tw);
+      if (tid < nwords + 1) pw[tid] = ew;
     }
-    // ---- 4. filter the rest, compacting in place ----
+    // ---- 4. filter the rest of the slice, compacting in place, and
+    // histogram the survivors over the next round's first level ----
+    lo = T + 1;
+    range = hi - lo;
+    sft = bin_shift(bitlen(range));
+    hb ^= 1;
+    uint32_t* nh = hist + hb * kTotBins;
+    for (int q = tid; q < kTotBins; q += nt) nh[q] = 0;
+    __syncthreads();
     // Each step u of a warp stores its survivors contiguously (ballot
     // ranks) after the warp's offset (one scan over the warps' totals).
     int base = 0;
@@ -487,6 +598,7 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
         const bool keep = x < m && kv[u] > T && !killed(nb, footprint_of(nb, (uint32_t)kv[u]), cov, pw);
         bal[u] = __ballot_sync(kFull, keep);
         cnt += __popc(bal[u]);
+        if (keep) hist_add(nh, bin_of(kv[u], lo, range, sft));
       }
       int tot;
       int o = base + block_scan_warps(cnt, s_scan, tot);  // all loads of the chunk precede its stores
@@ -499,14 +611,13 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       base += tot;
     }
     m = base;
-    lo = T + 1;
-    range = hi - lo;
-    sft = bin_shift(bitlen(range));
+    if (tid < ncl) *cluster.map_shared_rank(&s_qm[rank], tid) = m;
   }
-  if (tid == 0) {
+  if (first && tid == 0) {
     J->tkcount[nb] = nk < kcap ? nk : kcap;
     if (nk > kcap) J->stats[kStatError] = 3;
   }
+  // After the last barrier no CTA reads or writes another's shared memory.
 }
 
 }  // namespace
@@ -521,10 +632,31 @@ cudaError_t configure_total() {
 
 cudaError_t launch_total_select(const JobDev* jobs, int njobs, bool wide, cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
-  const dim3 grid(kNumNb, njobs);
-  if (wide) k_total_select<true><<<grid, kTotThreads, TotalSmem::total, s>>>(jobs);
-  else k_total_select<false><<<grid, kTotThreads, TotalSmem::total, s>>>(jobs);
-  return cudaGetLastError();
+  // Clusters as wide as about two waves of CTAs allow: a single search
+  // streams its lists with kTotCl SMs each, a large batch one SM per list.
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  int ncl = kTotCl;
+  while (ncl > 1 && (int64_t)njobs * kNumNb * ncl > 2 * (int64_t)sms) ncl >>= 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kNumNb * ncl, njobs);
+  cfg.blockDim = dim3(kTotThreads);
+  cfg.dynamicSmemBytes = TotalSmem::total;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ncl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (wide) return cudaLaunchKernelEx(&cfg, k_total_select<true>, jobs);
+  return cudaLaunchKernelEx(&cfg, k_total_select<false>, jobs);
 }
 
 }  // namespace mlp

@@ -17,12 +17,12 @@
 //      the keys' offsets from the smallest, refined into the lowest bin when
 //      that bin alone is too full): every CTA histograms its slice and adds
 //      the cluster's histograms through distributed shared memory;
-//   2. gathers those keys (the smallest of the list) into the first CTA of
-//      the cluster; every CTA copies them and orders them by rank;
-//   3. resolves them in order with a conflict bit matrix (lexicographically
-//      first maximal independent set, as in the stage-3 merge; every CTA
-//      computes a share of the rows and stores them into all CTAs) and adds
-//      the kept ones to a position bitmap of the kept moves,
+//   2. gathers those keys (the smallest of the list) into every CTA of the
+//      cluster and orders them by rank (each CTA ranks a share);
+//   3. resolves them in order with a conflict bit matrix (every CTA computes
+//      a share of the rows and stores them into all CTAs; one warp runs the
+//      greedy over it) and adds the kept ones to a position bitmap of the
+//      kept moves,
 //   4. filters the rest of its slice against the bitmap, compacting in
 //      place, and histograms the survivors for the next threshold.
 // Every CTA resolves each batch itself, so each holds the same bitmap; only
@@ -209,31 +209,23 @@ __device__ __forceinline__ bool conflict(int nb, uint32_t x, uint32_t y) {
   return xa <= yb && ya <= xb;
 }
 
-// The batch by rank: srt[r] = the key with r smaller keys (keys are
-// distinct: each encodes its move).  A warp ranks RK keys at a time against
-// the whole batch.
+// The batch in key order: srt[r] = the key with r smaller keys (keys are
+// distinct: each encodes its move) and mab[r] its footprint.  This CTA ranks
+// keys rank, rank + ncl, ... (a warp per key) and stores them into every CTA
+// of the cluster.
 template <bool WIDE>
-__device__ void rank_sort(const typename TK<WIDE>::K* bat, typename TK<WIDE>::K* srt, int nbat) {
+__device__ void rank_share(cg::cluster_group& cluster, int nb, const typename TK<WIDE>::K* bat,
+                           typename TK<WIDE>::K* srt, uint32_t* mab, int nbat, int rank, int ncl) {
   using K = typename TK<WIDE>::K;
-  constexpr int RK = WIDE ? 4 : 8;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int x0 = wid * RK; x0 < nbat; x0 += nw * RK) {
-    K kx[RK];
-    int c[RK];
-#pragma unroll
-    for (int k = 0; k < RK; k++) {
-      kx[k] = x0 + k < nbat ? bat[x0 + k] : kmax_value<K>();
-      c[k] = 0;
-    }
-    for (int y = lane; y < nbat; y += 32) {
-      const K ky = bat[y];
-#pragma unroll
-      for (int k = 0; k < RK; k++) c[k] += ky < kx[k] ? 1 : 0;
-    }
-#pragma unroll
-    for (int k = 0; k < RK; k++) {
-      const int r = (int)__reduce_add_sync(kFull, (unsigned)c[k]);
-      if (lane == k && x0 + k < nbat) srt[r] = kx[k];
+  for (int x = rank + ncl * wid; x < nbat; x += ncl * nw) {
+    const K kx = bat[x];
+    int c = 0;
+    for (int y = lane; y < nbat; y += 32) c += bat[y] < kx ? 1 : 0;
+    const int r = (int)__reduce_add_sync(kFull, (unsigned)c);
+    if (lane < ncl) {
+      *cluster.map_shared_rank(srt + r, lane) = kx;
+      *cluster.map_shared_rank(mab + r, lane) = footprint_of(nb, (uint32_t)kx);
     }
   }
 }
@@ -265,43 +257,42 @@ __device__ void conflict_rows(cg::cluster_group& cluster, int nb, const uint32_t
   }
 }
 
-// Lexicographically first maximal independent set of the batch's conflict
-// matrix, by rounds: a member whose earlier conflicting members are all
-// decided out joins; one that conflicts with a member in leaves.
-__device__ void resolve_rows(const uint32_t* bits, volatile uint8_t* mst, uint32_t* s_in, uint32_t* s_und, int na,
-                             int W) {
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-  for (int w = tid; w < W; w += nt) {
-    s_in[w] = 0;
-    const int rem = na - 32 * w;
-    s_und[w] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
-  }
-  __syncthreads();
-  for (int r = 0; r <= na; r++) {
-    int any = 0;
-    for (int x = tid; x < na; x += nt) {
-      if (mst[x] != kUndec) continue;
-      uint32_t hin = 0, hund = 0;
-      for (int w = 0; w <= (x >> 5); w++) {
-        const uint32_t row = bits[x * W + w];
-        hin |= row & s_in[w];
-        hund |= row & s_und[w];
+// Greedy over the batch in key order, by one warp (every lane calls it):
+// member x joins unless an earlier member that joined conflicts with it.
+// The members are taken 32 at a time (lane l: member 32 b + l); the earlier
+// blocks are decided, so a member conflicting with one of their kept members
+// leaves at once, and the rest of the block is settled by rounds of ballots
+// (a member joins once every earlier conflicting member of its block has
+// left).  The kept masks of the blocks stay in registers.  On return mst[x]
+// is kIn or kOut for every x < na.
+__device__ void warp_greedy_sorted(const uint32_t* bits, int W, int na, volatile uint8_t* mst) {
+  const int lane = threadIdx.x & 31;
+  uint32_t in[kTotBatch / 32];
+#pragma unroll
+  for (int b = 0; b < kTotBatch / 32; b++) {
+    in[b] = 0u;
+    if (b < W) {
+      const int x = 32 * b + lane;
+      const bool valid = x < na;
+      uint32_t ext = 0u, diag = 0u;
+      if (valid) {
+#pragma unroll
+        for (int w = 0; w < b; w++) ext |= bits[x * W + w] & in[w];
+        diag = bits[x * W + b];
       }
-      if (hin) mst[x] = kOut;
-      else if (!hund) mst[x] = kIn;
-      else any = 1;
-    }
-    __syncthreads();
-    for (int w = wid; w < W; w += nw) {
-      const int x = 32 * w + lane;
-      const uint8_t sx = x < na ? mst[x] : kNone;
-      const uint32_t bi = __ballot_sync(kFull, sx == kIn), bu = __ballot_sync(kFull, sx == kUndec);
-      if (lane == 0) {
-        s_in[w] = bi;
-        s_und[w] = bu;
+      uint8_t st = !valid ? kNone : (ext ? kOut : kUndec);
+      uint32_t und = __ballot_sync(kFull, st == kUndec), inb = 0u;
+      while (und) {  // every round settles at least the first undecided member
+        if (st == kUndec) {
+          if (diag & inb) st = kOut;
+          else if (!(diag & und)) st = kIn;
+        }
+        inb = __ballot_sync(kFull, st == kIn);
+        und = __ballot_sync(kFull, st == kUndec);
       }
+      in[b] = inb;
+      if (valid) mst[x] = st;
     }
-    if (!__syncthreads_or(any)) break;
   }
 }
 
@@ -337,7 +328,6 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
   __shared__ int s_qm[kTotCl];                // keys left in each CTA's slice, stored by that CTA
   __shared__ int s_scan[32];
   __shared__ int s_g, s_nbat, s_nb;
-  __shared__ uint32_t s_in[kTotBatch / 32], s_und[kTotBatch / 32];
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank(), ncl = (int)cluster.num_blocks();
   const bool first = rank == 0;
@@ -376,7 +366,6 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
   uint32_t* bits = (uint32_t*)(tsm + TotalSmem::bits);
   uint32_t* mab = (uint32_t*)(tsm + TotalSmem::ab);
   volatile uint8_t* mst = (volatile uint8_t*)(tsm + TotalSmem::st);
-  K* l_bat = cluster.map_shared_rank(bat, 0);
   int* l_nbat = cluster.map_shared_rank(&s_nbat, 0);
   const int nwords = (sz >> 5) + 2;  // bitmap words read for positions 0 .. sz
   for (int w = tid; w < kCovWords; w += nt) {
@@ -486,7 +475,7 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
       }
       if (!have_t) T = hi;  // unreachable: single-key bins always fit
     }
-    // ---- 2. the keys <= T go to the first CTA; every CTA copies them ----
+    // ---- 2. the keys <= T go to every CTA (slots counted by the first) ----
     for (int x0 = 0; x0 < m; x0 += U * nt) {
       K kv[U];
 #pragma unroll
@@ -504,7 +493,8 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
           if (lane == src) base = atomicAdd(l_nbat, __popc(bal));
           base = __shfl_sync(kFull, base, src);
           const int q = base + __popc(bal & ((1u << lane) - 1u));
-          if (g && q < kTotBatch) l_bat[q] = kv[u];
+          if (g && q < kTotBatch)
+            for (int c = 0; c < ncl; c++) *cluster.map_shared_rank(bat + q, c) = kv[u];
         }
       }
     }
@@ -517,21 +507,14 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
     __syncthreads();
     const int na = s_nb;
     const int W = (na + 31) >> 5;
-    if (!first)
-      for (int x = tid; x < na; x += nt) bat[x] = l_bat[x];
-    __syncthreads();
     // ---- 3. resolve the batch in key order ----
-    rank_sort<WIDE>(bat, srt, na);
-    __syncthreads();
-    for (int x = tid; x < na; x += nt) {
-      mab[x] = footprint_of(nb, (uint32_t)srt[x]);
-      mst[x] = kUndec;
-    }
-    __syncthreads();
+    rank_share<WIDE>(cluster, nb, bat, srt, mab, na, rank, ncl);
+    cluster.sync();  // every CTA holds the batch in key order
+    if (first && tid == 0) s_nbat = 0;  // every read of it precedes the barrier
     conflict_rows(cluster, nb, mab, bits, na, W, rank, ncl);
     cluster.sync();  // every CTA holds the whole conflict matrix
-    if (first && tid == 0) s_nbat = 0;  // every read of it precedes the barrier
-    resolve_rows(bits, mst, s_in, s_und, na, W);
+    if (tid < 32) warp_greedy_sorted(bits, W, na, mst);
+    __syncthreads();
     // Kept members, in key order, to the output region.
     const bool kin = tid < na && mst[tid] == kIn;
     int nin;

@@ -819,8 +819,10 @@ __device__ __forceinline__ void warp_lfmis(int c, int W, const uint32_t* bits, v
 // after the sort at :256), i.e. the lexicographically-first maximal
 // independent set of the conflict graph.
 //   swap:      rounds of "roots" (no earlier undecided/kept conflicting move)
-//              using per-position tables of the smallest key with an endpoint
-//              there (f_canSwapMerge conflicts are endpoints within 1).
+//              using per-position tables of the smallest undecided key and
+//              the smallest kept key with an endpoint there (f_canSwapMerge
+//              conflicts are endpoints within 1); a kept key enters its table
+//              once, when it is decided.
 //   2-opt, Or-opt: conflicts are closed-interval intersections and kept sets
 //              are small: the first alive candidate is kept and its conflicts
 //              removed, repeatedly.
@@ -842,14 +844,10 @@ __device__ __forceinline__ void stage2_group(int nb, int sz, int m, int gtid, in
       uint64_t* nxt = (round & 1) ? minB : minB2;
       for (int x = gtid; x < m; x += gnt) {
         const Rec r = rec[x];
-        if (r.st != kUndec && r.st != kIn) continue;
+        if (r.st != kUndec) continue;
         const int i = (int)(r.ab & 0xffff), j = (int)(r.ab >> 16);
         amin(&cur[i], r.key);
         amin(&cur[j], r.key);
-        if (r.st == kIn) {
-          amin(&minK[i], r.key);
-          amin(&minK[j], r.key);
-        }
       }
       group_sync(bar, gnt);
       int any = 0;
@@ -864,9 +862,17 @@ __device__ __forceinline__ void stage2_group(int nb, int sz, int m, int gtid, in
           qB = min(qB, min(cur[i + e], cur[j + e]));
           qK = min(qK, min(minK[i + e], minK[j + e]));
         }
-        if (qK < r.key) rec[x].st = kOut;
-        else if (qB >= r.key) rec[x].st = kIn;
-        else any = 1;
+        if (qK < r.key) {
+          rec[x].st = kOut;
+        } else if (qB >= r.key) {
+          // Kept: its key joins the kept table once.  A later candidate that
+          // misses it in this pass still saw this one as undecided in cur.
+          rec[x].st = kIn;
+          amin(&minK[i], r.key);
+          amin(&minK[j], r.key);
+        } else {
+          any = 1;
+        }
       }
       if (!group_sync_or(any, bar, gnt)) break;
     }

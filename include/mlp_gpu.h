@@ -235,6 +235,17 @@ MLP_API int mlp_tuning_get(int32_t* max_size, int32_t* shape_one, int32_t* shape
 MLP_API int mlp_tuning_load(const char* path);
 /* Autotune the sweep tile shape on the current tour; returns the chosen index. */
 MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape);
+/* Timing helper: `repeats` launches of the solver's sweep kernel for nb_mask
+ * on the current tour (improving candidates only, as its DVND iterations run
+ * it), timed with CUDA events on the solver's stream.  Without flush (null):
+ * the launches back to back between two events, *ms = the time per launch in
+ * milliseconds.  With flush (a device buffer of flush_bytes): the buffer is
+ * overwritten before every launch, so one larger than L2 makes each launch
+ * start cold, and each launch sits between its own two events; *ms = the
+ * median.  The candidate keys are reset and the ADS rebuilt afterwards; the
+ * tour is not changed. */
+MLP_API int mlp_solver_time_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats, void* flush, int64_t flush_bytes,
+                                  float* ms);
 
 /* Evaluation without any allocation (no counterpart in the reference).
  * For callers that cannot allocate device memory -- code running inside

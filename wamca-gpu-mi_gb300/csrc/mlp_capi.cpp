@@ -691,6 +691,58 @@ MLP_API int mlp_solver_autotune(mlp_solver_t s, int32_t* shape) {
   return kOk;
 }
 
+MLP_API int mlp_solver_time_sweep(mlp_solver_t s, int32_t nb_mask, int32_t repeats, void* flush, int64_t flush_bytes,
+                                  float* ms) {
+  MLP_RANGE("mlp_solver_time_sweep");
+  if (!s || !ms) return arg_error("null argument");
+  if (repeats <= 0 || repeats > 4096) return arg_error("repeats must be in 1 .. 4096");
+  if (flush != nullptr && flush_bytes <= 0) return arg_error("flush_bytes must be positive");
+  cudaStream_t st = s->set->stream();
+  MLP_TRY(s->set->set_mask(nb_mask));
+  MLP_CUDA(launch_stats_begin(s->set->device_jobs(), 1, 1, st), "stats kernel");
+  for (int r = 0; r < 3; r++) MLP_TRY(s->set->sweep_kernel());
+  std::vector<cudaEvent_t> ev;
+  int rc = kOk;
+  for (int q = 0; rc == kOk && q < 2 * repeats; q++) {
+    cudaEvent_t e = nullptr;
+    rc = cuda_status(cudaEventCreate(&e), "event");
+    if (rc == kOk) ev.push_back(e);
+  }
+  std::vector<float> t;
+  if (flush != nullptr) {
+    // Cold: every launch after the flush, between its own two events.
+    for (int r = 0; rc == kOk && r < repeats; r++) {
+      rc = cuda_status(cudaMemsetAsync(flush, r & 0xff, (size_t)flush_bytes, st), "L2 flush");
+      if (rc == kOk) rc = cuda_status(cudaEventRecord(ev[2 * r], st), "event");
+      if (rc == kOk) rc = s->set->sweep_kernel();
+      if (rc == kOk) rc = cuda_status(cudaEventRecord(ev[2 * r + 1], st), "event");
+    }
+    if (rc == kOk) rc = cuda_status(cudaStreamSynchronize(st), "sync");
+    for (int r = 0; rc == kOk && r < repeats; r++) {
+      float x = 0;
+      rc = cuda_status(cudaEventElapsedTime(&x, ev[2 * r], ev[2 * r + 1]), "event");
+      t.push_back(x);
+    }
+  } else {
+    // Warm: the launches back to back between two events (each launch's
+    // set-up overlaps the previous one's run, as in a DVND), per launch.
+    rc = cuda_status(cudaEventRecord(ev[0], st), "event");
+    for (int r = 0; rc == kOk && r < repeats; r++) rc = s->set->sweep_kernel();
+    if (rc == kOk) rc = cuda_status(cudaEventRecord(ev[1], st), "event");
+    if (rc == kOk) rc = cuda_status(cudaStreamSynchronize(st), "sync");
+    float x = 0;
+    if (rc == kOk) rc = cuda_status(cudaEventElapsedTime(&x, ev[0], ev[1]), "event");
+    t.push_back(x / (float)repeats);
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  MLP_TRY(rc);
+  std::sort(t.begin(), t.end());
+  *ms = t[t.size() / 2];
+  MLP_TRY(s->set->prepare(false));
+  MLP_CUDA(cudaStreamSynchronize(st), "sync");
+  return kOk;
+}
+
 // ---------------------------------------------------------------- batch
 MLP_API int mlp_batch_create(int32_t wide, mlp_batch_t* out) {
   if (!out) return arg_error("null output handle");

@@ -125,6 +125,7 @@ def lib() -> C.CDLL:
         "mlp_solver_stats": (C.c_int, [vp, P(DvndStats)]),
         "mlp_solver_sweep": (C.c_int, [vp, i32, i32, P(i64)]),
         "mlp_solver_autotune": (C.c_int, [vp, P(i32)]),
+        "mlp_solver_time_sweep": (C.c_int, [vp, i32, i32, vp, C.c_int64, P(C.c_float)]),
         "mlp_eval_noalloc": (C.c_int, [vp, i32, vp, i32, i32, vp, vp, vp, vp]),
         "mlp_tuning_set": (C.c_int, [vp, vp, vp, i32]),
         "mlp_tuning_get": (C.c_int, [vp, vp, vp, i32, P(i32)]),
@@ -442,6 +443,17 @@ class Solver:
         s = C.c_int32()
         _check(lib().mlp_solver_autotune(self._h, C.byref(s)))
         return s.value
+
+    def time_sweep(self, nb_mask: int = NB_ALL, repeats: int = 20, flush_ptr: int = 0, flush_bytes: int = 0) -> float:
+        """Time (seconds) of one launch of the solver's sweep kernel, by CUDA
+        events on the solver's stream (mlp_solver_time_sweep): warm, the mean
+        of `repeats` back-to-back launches; with a flush buffer (device pointer
+        and size), overwritten before every launch, the median of launches
+        that each start cold."""
+        ms = C.c_float()
+        _check(lib().mlp_solver_time_sweep(self._h, nb_mask, repeats, C.c_void_p(flush_ptr or None), flush_bytes,
+                                           C.byref(ms)))
+        return ms.value * 1e-3
 
 
 def eval_noalloc(dist_dev: int, n: int, tour_dev: int, nb: int, wide: bool, cost_dev: int, i_dev: int,

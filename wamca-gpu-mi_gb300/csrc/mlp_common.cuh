@@ -311,6 +311,15 @@ struct JobDev {
 constexpr int kTermWords = 12;
 
 #ifdef __CUDACC__
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization (launch_pdl) may start while its stream predecessor still
+// runs: pdl_wait() returns once the predecessor has completed and its memory
+// operations are visible; pdl_launch_dependents() lets the stream successor,
+// if launched the same way, start early.  Both do nothing in an ordinary
+// launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Inputs of position p's terms: w[p..p+3] (zero at and beyond size), W[p],
 // Q[p] and A_k[p], all modulo 2^32.
 struct TermIn {

@@ -1168,6 +1168,10 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
   __shared__ int s_m3, s_cnt;
   __shared__ int s_kept[kNumNb];  // leader: the kept-move count of each stage-2 CTA
   __shared__ JobDev s_job;        // leader: its copy of the job descriptor
+  // The next sweep may be launched now: it waits for this merge to end
+  // before it reads anything.  Before pdl_wait this kernel reads only what
+  // the sweep it follows does not write (statistics, tour, w).
+  pdl_launch_dependents();
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const JobDev* J = jobs + blockIdx.x / kClusterCtas;
@@ -1204,6 +1208,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
       t_old[p] = tour[p];
       if (w_old != nullptr) w_old[p] = w_cur[p];
     }
+    pdl_wait();
     cluster_wait();            // phase 1
     cluster_arrive_relaxed();  // phase 2: the leader has nothing to publish
     cluster_wait();            // phase 2 (acquire): the five kept lists and counts
@@ -1211,6 +1216,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kMergeThr
     cluster_arrive_relaxed();  // phase 1: this CTA runs
     const int nb = rank;
     int count = 0;
+    pdl_wait();  // the sweep's keys
     if ((mask >> nb) & 1) {
       const int m = nb_blocks(nb, sz);
       Rec* rec = (Rec*)ws;
@@ -1361,11 +1367,13 @@ __global__ void __launch_bounds__(kSoloThreads) k_merge_solo(const JobDev* __res
   extern __shared__ __align__(16) uint8_t dsm[];
   __shared__ uint64_t s_gmin[64];
   __shared__ int s_m3;
+  pdl_launch_dependents();  // as in k_merge
   const JobDev* J = jobs + blockIdx.x;
   {
     const int64_t* stt = J->stats;
     if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;
   }
+  pdl_wait();  // the sweep's keys
   const int sz = J->size, mask = J->nb_mask, tid = threadIdx.x, nt = blockDim.x;
   const SoloLayout lay(sz);
   uint8_t* ws = use_smem ? dsm : J->ws;
@@ -1904,13 +1912,11 @@ cudaError_t launch_merge(const JobDev* jobs, int njobs, bool wide, bool use_smem
   const size_t smem = use_smem ? MergeLayout(max_size).total : 0;
   const unsigned g = (unsigned)(njobs * kClusterCtas);
   if (wide) {
-    if (use_smem) k_merge<true, true><<<g, kMergeThreads, smem, s>>>(jobs);
-    else k_merge<true, false><<<g, kMergeThreads, smem, s>>>(jobs);
-  } else {
-    if (use_smem) k_merge<false, true><<<g, kMergeThreads, smem, s>>>(jobs);
-    else k_merge<false, false><<<g, kMergeThreads, smem, s>>>(jobs);
+    if (use_smem) return launch_pdl(k_merge<true, true>, dim3(g), dim3(kMergeThreads), smem, s, jobs);
+    return launch_pdl(k_merge<true, false>, dim3(g), dim3(kMergeThreads), smem, s, jobs);
   }
-  return cudaGetLastError();
+  if (use_smem) return launch_pdl(k_merge<false, true>, dim3(g), dim3(kMergeThreads), smem, s, jobs);
+  return launch_pdl(k_merge<false, false>, dim3(g), dim3(kMergeThreads), smem, s, jobs);
 }
 
 cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use_smem, int max_size,
@@ -1918,13 +1924,11 @@ cudaError_t launch_merge_solo(const JobDev* jobs, int njobs, bool wide, bool use
   if (njobs <= 0) return cudaSuccess;
   const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
   if (wide) {
-    if (use_smem) k_merge_solo<true, true><<<njobs, kSoloThreads, smem, s>>>(jobs);
-    else k_merge_solo<true, false><<<njobs, kSoloThreads, smem, s>>>(jobs);
-  } else {
-    if (use_smem) k_merge_solo<false, true><<<njobs, kSoloThreads, smem, s>>>(jobs);
-    else k_merge_solo<false, false><<<njobs, kSoloThreads, smem, s>>>(jobs);
+    if (use_smem) return launch_pdl(k_merge_solo<true, true>, dim3(njobs), dim3(kSoloThreads), smem, s, jobs);
+    return launch_pdl(k_merge_solo<true, false>, dim3(njobs), dim3(kSoloThreads), smem, s, jobs);
   }
-  return cudaGetLastError();
+  if (use_smem) return launch_pdl(k_merge_solo<false, true>, dim3(njobs), dim3(kSoloThreads), smem, s, jobs);
+  return launch_pdl(k_merge_solo<false, false>, dim3(njobs), dim3(kSoloThreads), smem, s, jobs);
 }
 
 cudaError_t launch_loop_condition(const JobDev* jobs, int njobs, cudaGraphConditionalHandle h,

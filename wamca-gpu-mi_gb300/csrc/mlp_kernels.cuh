@@ -20,6 +20,27 @@ constexpr TileShape kTileShapes[] = {{32, 4, 1},  {32, 8, 1},  {32, 16, 1}, {64,
                                        {64, 8, 2},  {64, 16, 2}, {64, 32, 2},  {128, 16, 2}};
 constexpr int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
 
+// Launches `kernel` with programmatic stream serialization on a created
+// stream (an ordinary launch on the legacy default stream): it may start
+// while its predecessor runs, once that predecessor calls
+// pdl_launch_dependents, and must call pdl_wait before it reads anything the
+// predecessor writes.  In a captured graph the dependency becomes a
+// programmatic edge.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = s != 0 ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // Bytes of dynamic shared memory the merge kernel needs for `size`
 // (0 if the job must use its global workspace instead).
 size_t merge_smem_bytes(int size);

@@ -84,6 +84,10 @@ __global__ void __launch_bounds__(TL) k_sweep_dvnd(const SweepTile* __restrict__
   const int32_t* __restrict__ D = J->D;
   const int4* __restrict__ RT = reinterpret_cast<const int4*>(J->RT);
   const int4* __restrict__ CT = reinterpret_cast<const int4*>(J->CT);
+  // The previous merge's tour, prefix arrays, statistics and key reset are
+  // complete past this point; the next merge may then be launched.
+  pdl_wait();
+  pdl_launch_dependents();
   const bool done = stats[kStatConverged] || stats[kStatSweeps] >= stats[kStatLimit];
   {
     // Tour entries of the tile's rows and columns and the term words of its
@@ -329,6 +333,10 @@ __global__ void __launch_bounds__(TLD / 2) k_sweep_dvnd2(const SweepTile* __rest
   const int32_t* __restrict__ D = J->D;
   const int4* __restrict__ RT = reinterpret_cast<const int4*>(J->RT);
   const int4* __restrict__ CT = reinterpret_cast<const int4*>(J->CT);
+  // The previous merge's tour, prefix arrays, statistics and key reset are
+  // complete past this point; the next merge may then be launched.
+  pdl_wait();
+  pdl_launch_dependents();
   const bool done = stats[kStatConverged] || stats[kStatSweeps] >= stats[kStatLimit];
   {
     constexpr int kSR = (SR + NTH - 1) / NTH, kNT = (NT + NTH - 1) / NTH;
@@ -541,17 +549,15 @@ __global__ void __launch_bounds__(TLD / 2) k_sweep_dvnd2(const SweepTile* __rest
 
 template <int TL, int TR>
 cudaError_t sweep_dvnd_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool local, cudaStream_t s) {
-  if (local) k_sweep_dvnd<TL, TR, true><<<ntiles, TL, 0, s>>>(tiles, jobs);
-  else k_sweep_dvnd<TL, TR, false><<<ntiles, TL, 0, s>>>(tiles, jobs);
-  return cudaGetLastError();
+  if (local) return launch_pdl(k_sweep_dvnd<TL, TR, true>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);
+  return launch_pdl(k_sweep_dvnd<TL, TR, false>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);
 }
 
 }  // namespace
 
 template <int TLD, int TR>
 cudaError_t sweep_dvnd2_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, cudaStream_t s) {
-  k_sweep_dvnd2<TLD, TR><<<ntiles, TLD / 2, 0, s>>>(tiles, jobs);
-  return cudaGetLastError();
+  return launch_pdl(k_sweep_dvnd2<TLD, TR>, dim3(ntiles), dim3(TLD / 2), 0, s, tiles, jobs);
 }
 
 cudaError_t launch_sweep_dvnd(const SweepTile* tiles, int ntiles, const JobDev* jobs, int shape, bool local,

@@ -122,11 +122,12 @@ MLP_API void mlp_solver_destroy(mlp_solver_t s);
 MLP_API int mlp_solver_set_stream(mlp_solver_t s, void* cuda_stream);
 /* Sweep tile shape index (0..13: diagonals x rows = 32x4, 32x8, 32x16, 64x4, 64x8,
  * 64x16, 128x8, 128x16, 32x32, 64x32, then 64x8, 64x16, 64x32, 128x16 where the
- * DVND sweep gives each thread two adjacent diagonals).  Loop mode of mlp_solver_dvnd: iterations >= 1
- * (default 16) replays CUDA graphs of that many iterations and checks
- * convergence on the host in between; iterations = 0 runs the whole loop on
- * the device (a CUDA-graph while node, no host round trips; always the mode
- * of mlp_solver_dvnd_async). */
+ * DVND sweep gives each thread two adjacent diagonals).  Loop mode of mlp_solver_dvnd: iterations = 0
+ * (the default) runs the whole loop on the device (a CUDA-graph while node
+ * over 16 iterations at a time, no host round trips; always the mode of
+ * mlp_solver_dvnd_async; a solver without a stream of its own checks on the
+ * host after every iteration); iterations >= 1 replays CUDA graphs of that
+ * many iterations and checks convergence on the host in between. */
 MLP_API int mlp_solver_set_tile_shape(mlp_solver_t s, int32_t shape);
 MLP_API int mlp_solver_set_unroll(mlp_solver_t s, int32_t iterations);
 /* DVND sweep kernel (no counterpart in the reference): 1 (default) the

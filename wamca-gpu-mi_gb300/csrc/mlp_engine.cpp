@@ -547,6 +547,12 @@ JobSet::~JobSet() {
   if (djobs_) cudaFree(djobs_);
   if (dtiles_) cudaFree(dtiles_);
   if (hstats_) cudaFreeHost(hstats_);
+  if (hstats2_) cudaFreeHost(hstats2_);
+  for (int b = 0; b < 2; b++) {
+    if (stats_ev_[b]) cudaEventDestroy(stats_ev_[b]);
+    if (htiles_[b]) cudaFreeHost(htiles_[b]);
+    if (hjobs_[b]) cudaFreeHost(hjobs_[b]);
+  }
   if (dstats_) cudaFree(dstats_);
   for (void* p : extra_ws_) cudaFree(p);
 }
@@ -578,48 +584,71 @@ int JobSet::init() {
   }
   MLP_CUDA(configure_merge(merge_smem_ ? merge_smem_bytes(max_size_) : 0), "configure merge");
   MLP_CUDA(cudaMallocHost(&hstats_, sizeof(int64_t) * kStatWords * jobs_.size()), "cudaMallocHost");
+  MLP_CUDA(cudaMallocHost(&hstats2_, sizeof(int64_t) * kStatWords * jobs_.size()), "cudaMallocHost");
+  for (int b = 0; b < 2; b++) {
+    MLP_CUDA(cudaEventCreateWithFlags(&stats_ev_[b], cudaEventDisableTiming), "event");
+    MLP_CUDA(cudaMallocHost(&hjobs_[b], sizeof(JobDev) * jobs_.size()), "cudaMallocHost");
+  }
   MLP_CUDA(cudaMalloc(&dstats_, sizeof(int64_t) * kStatWords * jobs_.size()), "cudaMalloc(stats)");
   MLP_CUDA(cudaMemset(dstats_, 0, sizeof(int64_t) * kStatWords * jobs_.size()), "memset(stats)");
   MLP_CUDA(cudaMalloc(&djobs_, sizeof(JobDev) * jobs_.size()), "cudaMalloc(jobs)");
-  std::vector<JobDev> h(jobs_.size());
+  JobDev* h = hjobs_[0];
   for (size_t q = 0; q < jobs_.size(); q++) {
     jobs_[q]->dev.stats = dstats_ + q * kStatWords;
     jobs_[q]->dev.RT = local_terms() ? nullptr : jobs_[q]->rt_mem;
     jobs_[q]->dev.CT = local_terms() ? nullptr : jobs_[q]->ct_mem;
     h[q] = jobs_[q]->dev;
   }
-  MLP_CUDA(cudaMemcpyAsync(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice, stream_),
+  MLP_CUDA(cudaMemcpyAsync(djobs_, h, sizeof(JobDev) * jobs_.size(), cudaMemcpyHostToDevice, stream_),
            "copy jobs");
   MLP_CUDA(cudaStreamSynchronize(stream_), "copy jobs");
   if (shape_ < 0) shape_ = default_shape(max_size_, (int)jobs_.size());
   return build_tiles();
 }
 
-int JobSet::build_tiles() {
+int JobSet::build_tiles(int buf, bool sync) {
   const TileShape ts = kTileShapes[shape_];
-  std::vector<SweepTile> tiles;
+  size_t count = 0;
   for (size_t q = 0; q < jobs_.size(); q++) {
     const int sz = jobs_[q]->size;
-    for (int rb = 0; rb < sweep_row_blocks(sz, ts.tr); rb++) {
-      const int r0 = 1 + rb * ts.tr;
-      for (int c = 0; c < sweep_row_tiles(sz, r0, ts.tl); c++)
-        tiles.push_back(SweepTile{(int32_t)q, r0, 1 + c * ts.tl, 0});
-    }
+    for (int rb = 0; rb < sweep_row_blocks(sz, ts.tr); rb++) count += (size_t)sweep_row_tiles(sz, 1 + rb * ts.tr, ts.tl);
   }
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
   if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
   loop_graph_ = nullptr;
-  if (dtiles_) cudaFree(dtiles_);
-  dtiles_ = nullptr;
-  ntiles_ = (int)tiles.size();
-  MLP_CUDA(cudaMalloc(&dtiles_, sizeof(SweepTile) * std::max<size_t>(1, tiles.size())), "cudaMalloc(tiles)");
-  MLP_CUDA(cudaMemcpy(dtiles_, tiles.data(), sizeof(SweepTile) * tiles.size(), cudaMemcpyHostToDevice),
-           "copy tiles");
+  if (count > tiles_cap_ || dtiles_ == nullptr) {
+    // Grow (the set's first build, or more jobs or smaller tiles than before).
+    MLP_CUDA(cudaStreamSynchronize(stream_), "grow tiles");
+    if (dtiles_) cudaFree(dtiles_);
+    dtiles_ = nullptr;
+    for (int b = 0; b < 2; b++) {
+      if (htiles_[b]) cudaFreeHost(htiles_[b]);
+      htiles_[b] = nullptr;
+    }
+    tiles_cap_ = 0;
+    const size_t cap = std::max<size_t>(1, count);
+    MLP_CUDA(cudaMalloc(&dtiles_, sizeof(SweepTile) * cap), "cudaMalloc(tiles)");
+    for (int b = 0; b < 2; b++) MLP_CUDA(cudaMallocHost(&htiles_[b], sizeof(SweepTile) * cap), "cudaMallocHost(tiles)");
+    tiles_cap_ = cap;
+  }
+  SweepTile* h = htiles_[buf];
+  size_t k = 0;
+  for (size_t q = 0; q < jobs_.size(); q++) {
+    const int sz = jobs_[q]->size;
+    for (int rb = 0; rb < sweep_row_blocks(sz, ts.tr); rb++) {
+      const int r0 = 1 + rb * ts.tr;
+      for (int c = 0; c < sweep_row_tiles(sz, r0, ts.tl); c++) h[k++] = SweepTile{(int32_t)q, r0, 1 + c * ts.tl, 0};
+    }
+  }
+  ntiles_ = (int)count;
+  if (count > 0)
+    MLP_CUDA(cudaMemcpyAsync(dtiles_, h, sizeof(SweepTile) * count, cudaMemcpyHostToDevice, stream_), "copy tiles");
+  if (sync) MLP_CUDA(cudaStreamSynchronize(stream_), "copy tiles");
   return kOk;
 }
 
-int JobSet::set_active(const std::vector<int>& idx) {
+int JobSet::set_active(const std::vector<int>& idx, int buf, bool sync) {
   std::vector<Job*> next;
   for (int q : idx) {
     if (q < 0 || q >= (int)all_jobs_.size()) {
@@ -631,12 +660,11 @@ int JobSet::set_active(const std::vector<int>& idx) {
   if (next == jobs_) return kOk;
   jobs_ = next;
   if (jobs_.empty()) return kOk;
-  std::vector<JobDev> h(jobs_.size());
+  JobDev* h = hjobs_[buf];
   for (size_t q = 0; q < jobs_.size(); q++) h[q] = jobs_[q]->dev;
-  MLP_CUDA(cudaMemcpyAsync(djobs_, h.data(), sizeof(JobDev) * h.size(), cudaMemcpyHostToDevice, stream_),
+  MLP_CUDA(cudaMemcpyAsync(djobs_, h, sizeof(JobDev) * jobs_.size(), cudaMemcpyHostToDevice, stream_),
            "copy jobs");
-  MLP_CUDA(cudaStreamSynchronize(stream_), "copy jobs");
-  return build_tiles();
+  return build_tiles(buf, sync);
 }
 
 int JobSet::ensure_all_active() {
@@ -869,6 +897,11 @@ int JobSet::enqueue_iterations(int iters) {
   return kOk;
 }
 
+// Iterations per pass of the device-side loop's body: the while node's
+// condition kernel runs once per pass, and a search that converges within a
+// pass leaves the rest of it as kernels that return at once.
+constexpr int kDeviceLoopBody = 16;
+
 int JobSet::enqueue_device_loop(int max_iters) {
   if (max_iters <= 0) {
     set_error("max_iters must be positive");
@@ -878,7 +911,7 @@ int JobSet::enqueue_device_loop(int max_iters) {
     set_error("the device-side loop needs a non-default stream");
     return kErrState;
   }
-  const int unroll = 2;
+  const int unroll = kDeviceLoopBody;
   if (!loop_graph_ || loop_unroll_ != unroll) {
     if (loop_graph_) cudaGraphExecDestroy(loop_graph_);
     loop_graph_ = nullptr;
@@ -956,6 +989,48 @@ int JobSet::run(int max_iters, bool sync) {
   for (size_t q = 0; q < active.size(); q++) active[q] = (int)q;
   int done = 0;
   int st = kOk;
+  if (!graphs && sync) {
+    // A batch checks one chunk late: chunk k + 1 is enqueued before the host
+    // waits for chunk k's statistics, so the device never waits for the
+    // host.  Jobs that converge meanwhile stay in one more chunk, whose
+    // kernels they leave at once; the new job and tile arrays go into the
+    // stream behind the chunk in flight, staged in pinned buffer b, which is
+    // staged into again only after the next check's wait (two chunks later).
+    int64_t* hst[2] = {hstats_, hstats2_};
+    const size_t sbytes = sizeof(int64_t) * kStatWords * all_jobs_.size();
+    int pend = -1, b = 0;
+    while (done < max_iters) {
+      const int u = std::min(unroll_, max_iters - done);
+      for (int q = 0; q < u && st == kOk; q++) st = launch_iteration();
+      if (st != kOk) break;
+      done += u;
+      st = cuda_status(cudaMemcpyAsync(hst[b], dstats_, sbytes, cudaMemcpyDeviceToHost, stream_), "read stats");
+      if (st == kOk) st = cuda_status(cudaEventRecord(stats_ev_[b], stream_), "read stats");
+      if (st != kOk) break;
+      if (pend >= 0) {
+        st = cuda_status(cudaEventSynchronize(stats_ev_[pend]), "read stats");
+        if (st == kOk) st = check_stats(hst[pend]);
+        if (st != kOk) break;
+        std::vector<int> next;
+        for (int q : active) {
+          const int64_t* sq = hst[pend] + (size_t)q * kStatWords;
+          if (!sq[kStatConverged] && sq[kStatSweeps] < max_iters) next.push_back(q);
+        }
+        if (next.empty()) break;
+        if (next.size() < active.size()) {
+          st = set_active(next, b, false);
+          if (st != kOk) break;
+          active.swap(next);
+        }
+      }
+      pend = b;
+      b ^= 1;
+    }
+    const int st1 = cuda_status(cudaStreamSynchronize(stream_), "batch loop");
+    if (st == kOk) st = st1;
+    const int st2 = ensure_all_active();
+    return st != kOk ? st : st2;
+  }
   while (done < max_iters) {
     const int u = std::min(unroll_, max_iters - done);
     if (graphs) {
@@ -991,8 +1066,12 @@ int JobSet::read_stats(std::vector<std::array<int64_t, kStatWords>>* out) {
   out->resize(all_jobs_.size());
   for (size_t q = 0; q < all_jobs_.size(); q++)
     std::memcpy((*out)[q].data(), hstats_ + q * kStatWords, sizeof(int64_t) * kStatWords);
+  return check_stats(hstats_);
+}
+
+int JobSet::check_stats(const int64_t* hst) {
   int64_t err = 0;
-  for (auto& a : *out) err |= a[kStatError];
+  for (size_t q = 0; q < all_jobs_.size(); q++) err |= hst[q * kStatWords + kStatError];
   if (err) {
     static const char* what[] = {"", "", "merge stage-2 hand-off timed out (no longer produced)", "kept-move region overflow",
                                  "TOTAL list overflow", "TOTAL selection invariant broken"};

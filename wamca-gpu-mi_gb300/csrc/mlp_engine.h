@@ -151,7 +151,10 @@ class JobSet {
   const std::vector<Job*>& jobs() const { return all_jobs_; }
   // Launch only the listed jobs (indices into jobs()); converged jobs are
   // dropped this way between graph replays of a batch.
-  int set_active(const std::vector<int>& idx);
+  // sync = false: the copies of the new job and tile arrays are left in the
+  // stream, staged in pinned buffer `buf` (0 or 1), which must not be staged
+  // into again before work enqueued after them has completed.
+  int set_active(const std::vector<int>& idx, int buf = 0, bool sync = true);
   int ensure_all_active();
   JobDev* device_jobs() const { return djobs_; }
   int ntiles() const { return ntiles_; }
@@ -172,7 +175,8 @@ class JobSet {
   int sweep_kernel_variant() const { return sweep_variant_; }
 
  private:
-  int build_tiles();
+  int build_tiles(int buf = 0, bool sync = true);
+  int check_stats(const int64_t* hst);  // the statistics' internal error words
   void drop_graphs();
   bool dvnd_sweep() const { return sweep_variant_ == 1 && !wide_ && mask_ == 0x1f; }
   // A set of one search computes the DVND sweep's row and column terms in
@@ -186,7 +190,7 @@ class JobSet {
   cudaStream_t stream_;
   int shape_ = -1;
   int unroll_ = 16;
-  bool device_loop_ = false;
+  bool device_loop_ = true;  // a one-search set on a stream loops on the device
   int mask_ = 0x1f;
   int max_size_ = 0;
   bool merge_smem_ = true;
@@ -199,6 +203,11 @@ class JobSet {
   SweepTile* dtiles_ = nullptr;
   int ntiles_ = 0;
   int64_t* hstats_ = nullptr;  // pinned, kStatWords per job
+  int64_t* hstats2_ = nullptr;  // a second one (the batch loop reads one while the other fills)
+  cudaEvent_t stats_ev_[2] = {nullptr, nullptr};
+  size_t tiles_cap_ = 0;                        // tiles dtiles_ and each staging buffer hold
+  SweepTile* htiles_[2] = {nullptr, nullptr};  // pinned staging of the tile list
+  JobDev* hjobs_[2] = {nullptr, nullptr};      // pinned staging of the job descriptors
   int64_t* dstats_ = nullptr;  // device, kStatWords per job (jobs' stats live here)
   std::vector<void*> extra_ws_;  // merge workspaces allocated for jobs of mixed-size sets
   std::map<int, cudaGraphExec_t> graphs_;

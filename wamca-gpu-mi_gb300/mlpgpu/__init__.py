@@ -309,6 +309,9 @@ class Solver:
         _check(lib().mlp_solver_set_tile_shape(self._h, shape))
 
     def set_unroll(self, u: int) -> None:
+        """Loop mode of dvnd(): 0 (default) the device-side loop (a CUDA-graph
+        while node, 16 iterations a pass); u >= 1 replays graphs of u
+        iterations and checks convergence on the host in between."""
         _check(lib().mlp_solver_set_unroll(self._h, u))
 
     def set_sweep_kernel(self, variant: int) -> None:

@@ -991,7 +991,7 @@ def main() -> None:
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-rates", default="250,500,1000,1500,2000,3000")
     ap.add_argument("--serve-slots", type=int, default=1024)
-    ap.add_argument("--serve-iters", type=int, default=2)
+    ap.add_argument("--serve-iters", type=int, default=8)  # DVND iterations per server step
     ap.add_argument("--large-n", type=int, default=10000)
     ap.add_argument("--large-iters", type=int, default=300)
     ap.add_argument("--total-reps", type=int, default=5)

@@ -305,8 +305,10 @@ MLP_API int mlp_batch_add_random_ties(mlp_batch_t b, mlp_problem_t p, uint32_t s
                                       int32_t* job);
 /* Candidate mode of the batch's searches (as mlp_solver_set_total). */
 MLP_API int mlp_batch_set_total(mlp_batch_t b, int32_t on);
-/* Iterations between the host's convergence checks (default 16); after each
- * check the jobs that converged leave the launches. */
+/* Iterations between the host's convergence checks (default 4); after each
+ * check the jobs that converged leave the launches.  The host reads each
+ * check's statistics while the next interval runs, so a job that converged
+ * stays in the launches for one more interval (its kernels return at once). */
 MLP_API int mlp_batch_set_check_interval(mlp_batch_t b, int32_t iterations);
 
 /* ---- serving form: continuous batching of arriving searches ----

@@ -37,7 +37,7 @@ struct mlp_batch {
   int mask = 0x1f;
   int merge_mode = 0;
   int sweep_kernel = 1;
-  int check_interval = 16;
+  int check_interval = 4;
   bool total = false;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;

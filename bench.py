@@ -363,12 +363,12 @@ def time_sweep(mlpgpu, solver, stream, flush, mask, reps):
     return solver.time_sweep(mask, reps, flush.data_ptr(), flush.numel() * flush.element_size())
 
 
-def plain_launches(sweeps: int, body: int = 16) -> int:
+def plain_launches(sweeps: int, body: int = 16, device_loop: bool = True) -> int:
     """Kernels one plain step enqueues: prepare of the new tour, statistics
-    reset, then passes of the device-side DVND loop, each `body` iterations
-    of (sweep, merge) and the while node's condition kernel, until the
-    condition sees convergence."""
-    return 2 + (2 * body + 1) * math.ceil(max(sweeps, 1) / body)
+    reset, then passes of `body` iterations of (sweep, merge) until
+    convergence is seen: by the while node's condition kernel after each
+    pass of the device-side loop, or by the host between graph replays."""
+    return 2 + (2 * body + (1 if device_loop else 0)) * math.ceil(max(sweeps, 1) / body)
 
 
 def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
@@ -381,6 +381,8 @@ def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
     prob = mlpgpu.Problem.from_coords(x, y, dist_round=True)
     solver = mlpgpu.Solver(prob, wide=False)
     solver.set_stream(stream.cuda_stream)
+    if args.dvnd_loop == "host":
+        solver.set_unroll(16)  # graph replays ncu can profile (same kernels)
     nsteps = args.warmup + args.steps
     tours = [workloads.random_perm_tour(n, 1_000 * rank + k) for k in range(nsteps)]
     tours_dev = torch.tensor(np.stack(tours), dtype=torch.int32, device="cuda")
@@ -894,7 +896,7 @@ def run_ours(args, world, rank, local) -> None:
     # The sweep runs warm inside the timed DVND (D and the tour's arrays stay
     # in L2 between iterations): its launch time there is the back-to-back one.
     achieved = sb / P["t_sweep_warm"] / 1e9
-    launches = sum(plain_launches(s) for s in P["step_sweeps"])
+    launches = sum(plain_launches(s, device_loop=args.dvnd_loop == "device") for s in P["step_sweeps"])
     traffic = ncu_traffic_per_sweep()
     step_ms = P["step_ms"]
     us_iter = 1e3 * sum(step_ms) / sum(P["step_sweeps"])
@@ -906,7 +908,8 @@ def run_ours(args, world, rank, local) -> None:
         "data": "synthetic (seeded uniform coordinates in [0,1000]^2, EUC_2D nint int32 distances)",
         "config": plain_config(args, world),
         "method": {"l2": "flushed (256 MB write) before every timed step", "tile_shape": P["shape"],
-                   "loop": "device-side loop: a CUDA-graph while node, 16 iterations a pass",
+                   "loop": ("device-side loop: a CUDA-graph while node, 16 iterations a pass"
+                            if args.dvnd_loop == "device" else "host-checked replays of 16-iteration CUDA graphs"),
                    "timing": "CUDA events on the solver's stream, inputs resident in HBM"},
         "dvnd_solves_per_s": solves,
         "latency_ms": {"p50": _pct(step_ms, 0.50), "p99": _pct(step_ms, 0.99), "mean": statistics.mean(step_ms)},
@@ -992,6 +995,9 @@ def main() -> None:
     ap.add_argument("--serve-rates", default="250,500,1000,1500,2000,3000")
     ap.add_argument("--serve-slots", type=int, default=1024)
     ap.add_argument("--serve-iters", type=int, default=8)  # DVND iterations per server step
+    # host: the plain steps replay 16-iteration graphs (ncu does not profile
+    # the kernel nodes of graphs with conditional nodes)
+    ap.add_argument("--dvnd-loop", choices=["device", "host"], default="device")
     ap.add_argument("--large-n", type=int, default=10000)
     ap.add_argument("--large-iters", type=int, default=300)
     ap.add_argument("--total-reps", type=int, default=5)

@@ -65,8 +65,10 @@ __device__ __forceinline__ void publish_diagonal(uint64_t* keys, int sz, int r0,
 // LOCAL: the tile computes its rows' and columns' terms from the prefix arrays
 // itself (a job set of one search: the ADS rebuild, on one SM, then writes no
 // term tables; here the work is spread over every tile).
-template <int TL, int TR, bool LOCAL>
-__global__ void __launch_bounds__(TL) k_sweep_dvnd(const SweepTile* __restrict__ tiles,
+// CAP: registers capped at 64 a thread (more CTAs resident per SM), for
+// grids that then fit in one wave when they otherwise would not.
+template <int TL, int TR, bool LOCAL, bool CAP = false>
+__global__ void __launch_bounds__(TL, CAP ? 1024 / TL : 1) k_sweep_dvnd(const SweepTile* __restrict__ tiles,
                                                    const JobDev* __restrict__ jobs) {
   constexpr int SR = TR + 3, SC = TL + 3, NT = TR + TL + 5, NCS = TL + TR - 1;
   __shared__ int32_t sS[SR][SC];
@@ -549,7 +551,30 @@ __global__ void __launch_bounds__(TLD / 2) k_sweep_dvnd2(const SweepTile* __rest
 
 template <int TL, int TR>
 cudaError_t sweep_dvnd_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, bool local, cudaStream_t s) {
-  if (local) return launch_pdl(k_sweep_dvnd<TL, TR, true>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);
+  if (local) {
+    // Tile-local terms (one search): shapes whose capped kernel does not
+    // spill take it when the grid then fits in one wave and otherwise needs
+    // a second.
+    if constexpr (TL >= 64 && TR <= 8) {
+      static int per_sm = -1, per_sm_cap = -1, sms = 0;
+      if (per_sm < 0) {
+        int dev = 0, a = 0, b = 0, c = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_sweep_dvnd<TL, TR, true, false>, TL, 0) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_sweep_dvnd<TL, TR, true, true>, TL, 0) == cudaSuccess) {
+          sms = c;
+          per_sm_cap = b;
+          per_sm = a;
+        } else {
+          per_sm = per_sm_cap = 0;  // no choice made: the plain kernel
+        }
+      }
+      if ((int64_t)ntiles > (int64_t)per_sm * sms && (int64_t)ntiles <= (int64_t)per_sm_cap * sms)
+        return launch_pdl(k_sweep_dvnd<TL, TR, true, true>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);
+    }
+    return launch_pdl(k_sweep_dvnd<TL, TR, true>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);
+  }
   return launch_pdl(k_sweep_dvnd<TL, TR, false>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);
 }
 

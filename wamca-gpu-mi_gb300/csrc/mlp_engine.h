@@ -124,8 +124,11 @@ class JobSet {
   int set_shape(int shape);
   int shape() const { return shape_; }
   int set_unroll(int u);
-  // true: DVND loops on the device (graph while-node); false: the host checks
-  // convergence after every `unroll` graph-replayed iterations.
+  // true (the default): a one-search set on a stream loops on the device
+  // (graph while node); false: the host checks convergence after every
+  // `unroll` graph-replayed iterations.  A batch always checks on the host,
+  // every `unroll` iterations, one check late (converged jobs then leave the
+  // launches).
   void set_device_loop(bool on) { device_loop_ = on; }
   // Rebuild the ADS arrays and reset statistics (after new tours).
   int prepare(bool reset_stats);
@@ -189,7 +192,7 @@ class JobSet {
   bool wide_;
   cudaStream_t stream_;
   int shape_ = -1;
-  int unroll_ = 16;
+  int unroll_ = 16;  // iterations between host checks (a batch's check interval)
   bool device_loop_ = true;  // a one-search set on a stream loops on the device
   int mask_ = 0x1f;
   int max_size_ = 0;

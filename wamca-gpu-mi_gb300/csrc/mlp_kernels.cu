@@ -364,8 +364,12 @@ __global__ void __launch_bounds__(TL) k_sweep(const SweepTile* __restrict__ tile
   const int32_t* __restrict__ Ag = J->A;
   const C* __restrict__ W = (const C*)J->W;
   const C* __restrict__ Q = (const C*)J->Q;
-  // Loaded with the tile's other independent loads; a job that converged or
-  // used its sweep limit is skipped before its distance gathers.
+  // In a programmatic launch (the TOTAL iteration's collecting sweep) the
+  // previous iteration has completed past this point; the TOTAL greedy may
+  // then be launched.  A job that converged or used its sweep limit is
+  // skipped before its distance gathers.
+  pdl_wait();
+  pdl_launch_dependents();
   const bool done = stats[kStatConverged] || stats[kStatSweeps] >= stats[kStatLimit];
 
   {
@@ -1562,11 +1566,13 @@ template <bool WIDE, bool SMEM>
 __global__ void __launch_bounds__(kMergeThreads) k_total_finish(const JobDev* __restrict__ jobs) {
   constexpr bool use_smem = SMEM;
   extern __shared__ __align__(16) uint8_t dsm[];
+  pdl_launch_dependents();  // the next collecting sweep waits for this kernel's end
   const JobDev* J = jobs + blockIdx.x;
   {
     const int64_t* stt = J->stats;
     if (stt[kStatConverged] || stt[kStatSweeps] >= stt[kStatLimit]) return;
   }
+  pdl_wait();  // the greedy's kept moves
   const int sz = J->size, mask = J->nb_mask, tid = threadIdx.x, nt = blockDim.x;
   const SoloLayout lay(sz);
   uint8_t* ws = use_smem ? dsm : J->ws;
@@ -1744,8 +1750,7 @@ __global__ void k_loop_condition(const JobDev* __restrict__ jobs, int njobs, cud
 
 template <bool WIDE, int TL, int TR>
 cudaError_t sweep_collect_launch(const SweepTile* tiles, int ntiles, const JobDev* jobs, cudaStream_t s) {
-  k_sweep<WIDE, TL, TR, true><<<ntiles, TL, 0, s>>>(tiles, jobs, 1);
-  return cudaGetLastError();
+  return launch_pdl(k_sweep<WIDE, TL, TR, true>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs, 1);
 }
 
 template <bool WIDE, int TL, int TR>
@@ -1842,13 +1847,11 @@ cudaError_t launch_total_finish(const JobDev* jobs, int njobs, bool wide, bool u
   if (njobs <= 0) return cudaSuccess;
   const size_t smem = use_smem ? SoloLayout(max_size).total : 0;
   if (wide) {
-    if (use_smem) k_total_finish<true, true><<<njobs, kMergeThreads, smem, s>>>(jobs);
-    else k_total_finish<true, false><<<njobs, kMergeThreads, smem, s>>>(jobs);
-  } else {
-    if (use_smem) k_total_finish<false, true><<<njobs, kMergeThreads, smem, s>>>(jobs);
-    else k_total_finish<false, false><<<njobs, kMergeThreads, smem, s>>>(jobs);
+    if (use_smem) return launch_pdl(k_total_finish<true, true>, dim3(njobs), dim3(kMergeThreads), smem, s, jobs);
+    return launch_pdl(k_total_finish<true, false>, dim3(njobs), dim3(kMergeThreads), smem, s, jobs);
   }
-  return cudaGetLastError();
+  if (use_smem) return launch_pdl(k_total_finish<false, true>, dim3(njobs), dim3(kMergeThreads), smem, s, jobs);
+  return launch_pdl(k_total_finish<false, false>, dim3(njobs), dim3(kMergeThreads), smem, s, jobs);
 }
 
 size_t oropt_pass_scratch_bytes(int size, int k) {

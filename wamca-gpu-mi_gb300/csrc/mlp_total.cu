@@ -328,6 +328,7 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
   __shared__ int s_qm[kTotCl];                // keys left in each CTA's slice, stored by that CTA
   __shared__ int s_scan[32];
   __shared__ int s_g, s_nbat, s_nb;
+  pdl_launch_dependents();  // the TOTAL finish waits for this kernel's end
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank(), ncl = (int)cluster.num_blocks();
   const bool first = rank == 0;
@@ -345,6 +346,7 @@ __global__ void __launch_bounds__(kTotThreads) k_total_select(const JobDev* __re
     if (first && tid == 0) J->tkcount[nb] = 0;
     return;
   }
+  pdl_wait();  // the collecting sweep's lists
   const int mall = J->tcount[nb];
   if (mall > total_list_cap(nb, sz)) {
     if (first && tid == 0) {
@@ -631,13 +633,16 @@ cudaError_t launch_total_select(const JobDev* jobs, int njobs, bool wide, cudaSt
   cfg.blockDim = dim3(kTotThreads);
   cfg.dynamicSmemBytes = TotalSmem::total;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = ncl;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  // Programmatic stream serialization (see launch_pdl) on a created stream.
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = s != 0 ? 2 : 1;
   if (wide) return cudaLaunchKernelEx(&cfg, k_total_select<true>, jobs);
   return cudaLaunchKernelEx(&cfg, k_total_select<false>, jobs);
 }

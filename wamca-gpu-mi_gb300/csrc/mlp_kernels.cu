@@ -1791,23 +1791,21 @@ size_t merge_ws_bytes(int size) {
 }
 size_t solo_smem_bytes(int size) { return SoloLayout(size).total; }
 int solo_smem_max_size() {
-  static int cached = 0;
-  if (cached == 0) {
+  static const int cached = [] {
     int sz = 8;
     while (sz < kMaxSize && SoloLayout(sz + 1).total <= (size_t)(227 * 1024 - 8192)) sz++;
-    cached = sz;
-  }
+    return sz;
+  }();
   return cached;
 }
 int merge_smem_max_size() {
   // Largest size whose merge workspace fits the 227 KB opt-in shared memory
   // (minus the kernel's static shared memory).
-  static int cached = 0;
-  if (cached == 0) {
+  static const int cached = [] {
     int sz = 8;
     while (sz < kMaxSize && MergeLayout(sz + 1).total <= kMergeSmemLimit) sz++;
-    cached = sz;
-  }
+    return sz;
+  }();
   return cached;
 }
 

@@ -556,21 +556,24 @@ cudaError_t sweep_dvnd_launch(const SweepTile* tiles, int ntiles, const JobDev* 
     // spill take it when the grid then fits in one wave and otherwise needs
     // a second.
     if constexpr (TL >= 64 && TR <= 8) {
-      static int per_sm = -1, per_sm_cap = -1, sms = 0;
-      if (per_sm < 0) {
+      // Resident CTAs per SM of both copies, and the SM count (queried once;
+      // without them, the plain kernel).
+      struct Fit {
+        int64_t one_wave = 0, one_wave_cap = 0;
+      };
+      static const Fit fit = [] {
+        Fit f;
         int dev = 0, a = 0, b = 0, c = 0;
         if (cudaGetDevice(&dev) == cudaSuccess &&
             cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_sweep_dvnd<TL, TR, true, false>, TL, 0) == cudaSuccess &&
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_sweep_dvnd<TL, TR, true, true>, TL, 0) == cudaSuccess) {
-          sms = c;
-          per_sm_cap = b;
-          per_sm = a;
-        } else {
-          per_sm = per_sm_cap = 0;  // no choice made: the plain kernel
+          f.one_wave = (int64_t)a * c;
+          f.one_wave_cap = (int64_t)b * c;
         }
-      }
-      if ((int64_t)ntiles > (int64_t)per_sm * sms && (int64_t)ntiles <= (int64_t)per_sm_cap * sms)
+        return f;
+      }();
+      if ((int64_t)ntiles > fit.one_wave && (int64_t)ntiles <= fit.one_wave_cap)
         return launch_pdl(k_sweep_dvnd<TL, TR, true, true>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);
     }
     return launch_pdl(k_sweep_dvnd<TL, TR, true>, dim3(ntiles), dim3(TL), 0, s, tiles, jobs);

@@ -619,13 +619,13 @@ cudaError_t launch_total_select(const JobDev* jobs, int njobs, bool wide, cudaSt
   if (njobs <= 0) return cudaSuccess;
   // Clusters as wide as about two waves of CTAs allow: a single search
   // streams its lists with kTotCl SMs each, a large batch one SM per list.
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-  }
+  // (SM count queried once; without it, clusters of one CTA.)
+  static const int sms = [] {
+    int dev = 0, c = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 0;
+    return c;
+  }();
   int ncl = kTotCl;
   while (ncl > 1 && (int64_t)njobs * kNumNb * ncl > 2 * (int64_t)sms) ncl >>= 1;
   cudaLaunchConfig_t cfg = {};

@@ -372,7 +372,7 @@ def plain_launches(sweeps: int, body: int = 16, device_loop: bool = True) -> int
 
 
 def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
-    """configs[1]: plain single instance, n = 1000 (the headline)."""
+    """The plain single-instance workload, n = 1000 (the headline)."""
     import torch
 
     n = N_NODES
@@ -443,7 +443,7 @@ def bench_plain(args, world, rank, mlpgpu, workloads, stream, flush):
 
 
 def bench_batched(args, mlpgpu, workloads, stream):
-    """configs[2]: 512 clustered instances, n log-uniform in [100, 1000], 4
+    """The batched workload: 512 clustered instances, n log-uniform in [100, 1000], 4
     seeded random starts each (2048 DVND searches) in one batch, against the
     plain form (one mlp_solver_dvnd per search) on a sample of the searches."""
     import torch
@@ -515,7 +515,7 @@ def bench_batched(args, mlpgpu, workloads, stream):
 
 
 def bench_serving(args, mlpgpu, workloads):
-    """configs[4]: open-loop Poisson stream of requests, n log-uniform in
+    """The serving workload: open-loop Poisson stream of requests, n log-uniform in
     [50, 2000], half uniform / half 8-cluster coordinates, each a full DVND
     from a seeded random start, admitted against a 40 GB device budget."""
     nreq = args.serve_requests
@@ -598,7 +598,7 @@ def bench_serving(args, mlpgpu, workloads):
 
 
 def bench_large(args, mlpgpu, workloads, stream, flush):
-    """configs[3]: n = 10000, int64 costs, D (400 MB) in HBM: one Or-opt-3 +
+    """The large workload: n = 10000, int64 costs, D (400 MB) in HBM: one Or-opt-3 +
     2-opt sweep against the HBM roofline, and a DVND capped in sweeps."""
     import torch
 

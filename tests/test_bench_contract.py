@@ -29,3 +29,17 @@ def test_reference_arm_json_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_plain_launch_count_matches_the_loop_modes():
+    # The gpu_launches claim of a plain step: prepare, statistics reset, then
+    # passes of 16 iterations of (sweep, merge), each with the while node's
+    # condition kernel in the device-side loop (the default) and without it in
+    # host-checked graph replays.
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.plain_launches(259) == 2 + 33 * 17
+    assert bench.plain_launches(259, device_loop=False) == 2 + 32 * 17
+    assert bench.plain_launches(16) == 2 + 33 and bench.plain_launches(17) == 2 + 66
+    assert bench.plain_launches(0) == bench.plain_launches(1) == 2 + 33
